@@ -1,0 +1,285 @@
+// k_match.cu -- matching-cost kernels (module form of seq/PixelBasedCost.cpp,
+// seq/CensusTransform.cpp, seq/RankFilter.cpp, seq/ConvolveImage.cpp,
+// seq/NCCDisparity.cpp, seq/CombineCost.cpp).
+//
+// Float arithmetic that must match the reference bit for bit is written with
+// explicit round-to-nearest intrinsics in the reference's order; the library
+// is compiled with -fmad=false so no multiply-add is fused behind our back.
+#include "rts_common.cuh"
+
+namespace rts {
+
+// ---------------------------------------------------------------------------
+// Absolute differences.  Grid: x-blocks over W*D of one row, y over rows; the
+// cost volume is written with d fastest, so consecutive threads store
+// consecutive floats.
+
+template <typename T>
+__global__ void k_ad_1ch(const T *__restrict__ ref, const T *__restrict__ tar, float *__restrict__ cost, int D,
+                         int H, int W, int dir) {
+    const int y = blockIdx.y;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= W * D) return;
+    const int x = i / D, d = i - x * D;
+    const int xt = tar_col(x, d, W, dir);
+    const size_t row = (size_t)y * W;
+    float v;
+    if constexpr (sizeof(T) == 1) {
+        // seq/PixelBasedCost.cpp:22 abs of an int difference
+        v = (float)abs((int)ref[row + x] - (int)tar[row + xt]);
+    } else {
+        // seq/PixelBasedCost.cpp:48-50 float difference then sign flip
+        v = __fsub_rn(ref[row + x], tar[row + xt]);
+        if (v < 0) v = -v;
+    }
+    cost[(row + x) * D + d] = v;
+}
+
+__global__ void k_ad_color(const uint8_t *__restrict__ ref, const uint8_t *__restrict__ tar,
+                           float *__restrict__ cost, int D, int H, int W, int dir, int use_trunc, float trunc,
+                           int norm) {
+    const int y = blockIdx.y;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= W * D) return;
+    const int x = i / D, d = i - x * D;
+    const int xt = tar_col(x, d, W, dir);
+    const size_t row = (size_t)y * W;
+    const uint8_t *a = ref + 3 * (row + x);
+    const uint8_t *b = tar + 3 * (row + xt);
+    const int sad = abs((int)a[0] - (int)b[0]) + abs((int)a[1] - (int)b[1]) + abs((int)a[2] - (int)b[2]);
+    // seq/PixelBasedCost.cpp:86-91,106-112: min(sad, trunc), then (float)1/(float)3 * v
+    float v = (float)sad;
+    if (use_trunc) v = (v > trunc) ? trunc : v;
+    if (norm) v = __fmul_rn(1.0f / 3.0f, v);
+    cost[(row + x) * D + d] = v;
+}
+
+// ---------------------------------------------------------------------------
+// Census.  Module form writes the reference's bool layout, one byte per bit;
+// the pipeline uses packed 64-bit words (bit k of the window in word k/64).
+
+__global__ void k_census_bits(const uint8_t *__restrict__ img, uint8_t *__restrict__ bits, int hr, int wr, int H,
+                              int W) {
+    const int y = blockIdx.y;
+    const int bw = 2 * wr + 1, nb = (2 * hr + 1) * bw;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= W * nb) return;
+    const int x = i / nb, k = i - x * nb;
+    const int dy = k / bw - hr, dx = k - (k / bw) * bw - wr;
+    const uint8_t c = img[(size_t)y * W + x];
+    const uint8_t n = img[(size_t)wrap1(y + dy, H) * W + wrap1(x + dx, W)];
+    bits[((size_t)y * W + x) * nb + k] = (c > n) ? 1 : 0;  // seq/CensusTransform.cpp:31 strict
+}
+
+template <int NW>
+__global__ void k_census_codes(const uint8_t *__restrict__ img, uint64_t *__restrict__ codes, int hr, int wr,
+                               int H, int W) {
+    const int y = blockIdx.y;
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= W) return;
+    const uint8_t c = img[(size_t)y * W + x];
+    uint64_t w[NW];
+#pragma unroll
+    for (int j = 0; j < NW; j++) w[j] = 0;
+    int k = 0;
+    for (int dy = -hr; dy <= hr; dy++) {
+        const uint8_t *row = img + (size_t)wrap1(y + dy, H) * W;
+        for (int dx = -wr; dx <= wr; dx++, k++) {
+            const uint64_t bit = (c > row[wrap1(x + dx, W)]) ? 1ull : 0ull;
+#pragma unroll
+            for (int j = 0; j < NW; j++)
+                if ((k >> 6) == j) w[j] |= bit << (k & 63);
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < NW; j++) codes[((size_t)y * W + x) * NW + j] = w[j];
+}
+
+template <int NW>
+__global__ void k_bits_pack(const uint8_t *__restrict__ bits, uint64_t *__restrict__ codes, int nb, long npix) {
+    const long p = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= npix) return;
+    const uint8_t *b = bits + (size_t)p * nb;
+    uint64_t w[NW];
+#pragma unroll
+    for (int j = 0; j < NW; j++) w[j] = 0;
+    for (int k = 0; k < nb; k++) {
+        const uint64_t bit = b[k] ? 1ull : 0ull;
+#pragma unroll
+        for (int j = 0; j < NW; j++)
+            if ((k >> 6) == j) w[j] |= bit << (k & 63);
+    }
+#pragma unroll
+    for (int j = 0; j < NW; j++) codes[(size_t)p * NW + j] = w[j];
+}
+
+template <int NW>
+__global__ void k_hamming(const uint64_t *__restrict__ cr, const uint64_t *__restrict__ ct, float *__restrict__ cost,
+                          int D, int H, int W) {
+    const int y = blockIdx.y;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= W * D) return;
+    const int x = i / D, d = i - x * D;
+    const int xt = tar_col(x, d, W, 1);
+    const size_t row = (size_t)y * W;
+    int cnt = 0;
+#pragma unroll
+    for (int j = 0; j < NW; j++) cnt += __popcll(cr[(row + x) * NW + j] ^ ct[(row + xt) * NW + j]);
+    cost[(row + x) * D + d] = (float)cnt;  // seq/CensusTransform.cpp:60
+}
+
+// ---------------------------------------------------------------------------
+// Rank transform (seq/RankFilter.cpp:11-35): 1 + #{q : I(q) < I(p)}, u8 wrap.
+__global__ void k_rank(const uint8_t *__restrict__ img, uint8_t *__restrict__ out, int m, int H, int W) {
+    const int y = blockIdx.y;
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= W) return;
+    const uint8_t c = img[(size_t)y * W + x];
+    int cnt = 1;
+    for (int dy = -m; dy <= m; dy++) {
+        const uint8_t *row = img + (size_t)wrap1(y + dy, H) * W;
+        for (int dx = -m; dx <= m; dx++) cnt += (row[wrap1(x + dx, W)] < c) ? 1 : 0;
+    }
+    out[(size_t)y * W + x] = (uint8_t)cnt;
+}
+
+// LoG convolution (seq/ConvolveImage.cpp:11-35): raster-order sum of rounded
+// products, |.|, min 255.
+__global__ void k_convolve(const uint8_t *__restrict__ img, float *__restrict__ out, const float *__restrict__ mask,
+                           int H, int W, int hr, int wr) {
+    const int y = blockIdx.y;
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= W) return;
+    const int mw = 2 * wr + 1;
+    float acc = 0.f;
+    for (int dy = -hr; dy <= hr; dy++) {
+        const uint8_t *row = img + (size_t)wrap1(y + dy, H) * W;
+        const float *mk = mask + (dy + hr) * mw + wr;
+        for (int dx = -wr; dx <= wr; dx++) acc = __fadd_rn(acc, __fmul_rn((float)row[wrap1(x + dx, W)], mk[dx]));
+    }
+    acc = (acc > 0.f) ? acc : -acc;
+    out[(size_t)y * W + x] = (acc > 255.f) ? 255.f : acc;
+}
+
+// Window mean for NCC (seq/NCCDisparity.cpp:24-35): raster-order float sum / area.
+// The target mean of (x, d) equals this mean at column x-d (wrapped): the same
+// pixels are summed in the same order.
+__global__ void k_window_mean(const uint8_t *__restrict__ img, float *__restrict__ mean, int H, int W, int hr,
+                              int wr) {
+    const int y = blockIdx.y;
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= W) return;
+    float s = 0.f;
+    for (int dy = -hr; dy <= hr; dy++) {
+        const uint8_t *row = img + (size_t)wrap1(y + dy, H) * W;
+        for (int dx = -wr; dx <= wr; dx++) s = __fadd_rn(s, (float)row[wrap1(x + dx, W)]);
+    }
+    mean[(size_t)y * W + x] = __fdiv_rn(s, (float)((2 * hr + 1) * (2 * wr + 1)));
+}
+
+// NCC (seq/NCCDisparity.cpp:50-71): nom = sum rv*tv, den = sqrtf(sum ((rv*rv)*tv)*tv);
+// the cell is written only when den != 0.
+__global__ void k_ncc(const uint8_t *__restrict__ ref, const uint8_t *__restrict__ tar,
+                      const float *__restrict__ mref, const float *__restrict__ mtar, float *__restrict__ cost,
+                      int D, int H, int W, int hr, int wr) {
+    const int y = blockIdx.y;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= W * D) return;
+    const int x = i / D, d = i - x * D;
+    const float mr = mref[(size_t)y * W + x];
+    const float mt = mtar[(size_t)y * W + wrap1(x - d, W)];
+    float nom = 0.f, den = 0.f;
+    for (int dy = -hr; dy <= hr; dy++) {
+        const size_t row = (size_t)wrap1(y + dy, H) * W;
+        for (int dx = -wr; dx <= wr; dx++) {
+            const float rv = __fsub_rn((float)ref[row + wrap1(x + dx, W)], mr);
+            const float tv = __fsub_rn((float)tar[row + wrap1(x + dx - d, W)], mt);
+            nom = __fadd_rn(nom, __fmul_rn(rv, tv));
+            den = __fadd_rn(den, __fmul_rn(__fmul_rn(__fmul_rn(rv, rv), tv), tv));
+        }
+    }
+    den = __fsqrt_rn(den);
+    if (den != 0.f) cost[((size_t)y * W + x) * D + d] = __fdiv_rn(nom, den);
+}
+
+// CombineCost (seq/CombineCost.cpp:11-25).  Integer-valued costs in range take
+// 1-expf(-v/lambda) from a table computed on the host with the C library's
+// expf (the reference's arithmetic); other values use the device expf.
+__device__ __forceinline__ float combine_term(float v, const float *__restrict__ lut, float lambda) {
+    if (v >= 0.f && v < (float)kCombineLut && v == truncf(v)) return lut[(int)v];
+    return __fsub_rn(1.0f, expf(__fdiv_rn(-v, lambda)));
+}
+
+__global__ void k_combine(float *__restrict__ c1, const float *__restrict__ c2, long n, const float *__restrict__ lut1,
+                          const float *__restrict__ lut2, float lambda1, float lambda2) {
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+        const float a = combine_term(c1[i], lut1, lambda1);
+        const float b = combine_term(c2[i], lut2, lambda2);
+        c1[i] = __fadd_rn(a, b);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// launchers
+
+static dim3 row_grid(long per_row, int H, int threads) { return dim3((unsigned)((per_row + threads - 1) / threads), H); }
+
+void launch_ad_gray(cudaStream_t s, const uint8_t *ref, const uint8_t *tar, float *cost, int D, int H, int W, int dir) {
+    k_ad_1ch<uint8_t><<<row_grid((long)W * D, H, 256), 256, 0, s>>>(ref, tar, cost, D, H, W, dir);
+}
+void launch_ad_float(cudaStream_t s, const float *ref, const float *tar, float *cost, int D, int H, int W, int dir) {
+    k_ad_1ch<float><<<row_grid((long)W * D, H, 256), 256, 0, s>>>(ref, tar, cost, D, H, W, dir);
+}
+void launch_ad_color(cudaStream_t s, const uint8_t *ref, const uint8_t *tar, float *cost, int D, int H, int W, int dir,
+                     int use_trunc, float trunc, int norm) {
+    k_ad_color<<<row_grid((long)W * D, H, 256), 256, 0, s>>>(ref, tar, cost, D, H, W, dir, use_trunc, trunc, norm);
+}
+void launch_census_bits(cudaStream_t s, const uint8_t *img, uint8_t *bits, int hr, int wr, int H, int W) {
+    const long nb = (long)(2 * hr + 1) * (2 * wr + 1);
+    k_census_bits<<<row_grid(W * nb, H, 256), 256, 0, s>>>(img, bits, hr, wr, H, W);
+}
+int census_words(int hr, int wr) {
+    const int nb = (2 * hr + 1) * (2 * wr + 1);
+    return nb <= 64 ? 1 : nb <= 128 ? 2 : nb <= 256 ? 4 : 0;
+}
+void launch_census_codes(cudaStream_t s, const uint8_t *img, uint64_t *codes, int hr, int wr, int H, int W) {
+    const dim3 g = row_grid(W, H, 128);
+    switch (census_words(hr, wr)) {
+    case 1: k_census_codes<1><<<g, 128, 0, s>>>(img, codes, hr, wr, H, W); break;
+    case 2: k_census_codes<2><<<g, 128, 0, s>>>(img, codes, hr, wr, H, W); break;
+    case 4: k_census_codes<4><<<g, 128, 0, s>>>(img, codes, hr, wr, H, W); break;
+    }
+}
+void launch_bits_pack(cudaStream_t s, const uint8_t *bits, uint64_t *codes, int nb, long npix) {
+    const unsigned g = (unsigned)((npix + 127) / 128);
+    if (nb <= 64) k_bits_pack<1><<<g, 128, 0, s>>>(bits, codes, nb, npix);
+    else if (nb <= 128) k_bits_pack<2><<<g, 128, 0, s>>>(bits, codes, nb, npix);
+    else k_bits_pack<4><<<g, 128, 0, s>>>(bits, codes, nb, npix);
+}
+void launch_hamming(cudaStream_t s, const uint64_t *cr, const uint64_t *ct, float *cost, int nw, int D, int H, int W) {
+    const dim3 g = row_grid((long)W * D, H, 256);
+    if (nw == 1) k_hamming<1><<<g, 256, 0, s>>>(cr, ct, cost, D, H, W);
+    else if (nw == 2) k_hamming<2><<<g, 256, 0, s>>>(cr, ct, cost, D, H, W);
+    else k_hamming<4><<<g, 256, 0, s>>>(cr, ct, cost, D, H, W);
+}
+void launch_rank(cudaStream_t s, const uint8_t *img, uint8_t *out, int m, int H, int W) {
+    k_rank<<<row_grid(W, H, 128), 128, 0, s>>>(img, out, m, H, W);
+}
+void launch_convolve(cudaStream_t s, const uint8_t *img, float *out, const float *mask, int H, int W, int hr, int wr) {
+    k_convolve<<<row_grid(W, H, 128), 128, 0, s>>>(img, out, mask, H, W, hr, wr);
+}
+void launch_window_mean(cudaStream_t s, const uint8_t *img, float *mean, int H, int W, int hr, int wr) {
+    k_window_mean<<<row_grid(W, H, 128), 128, 0, s>>>(img, mean, H, W, hr, wr);
+}
+void launch_ncc(cudaStream_t s, const uint8_t *ref, const uint8_t *tar, const float *mref, const float *mtar,
+                float *cost, int D, int H, int W, int hr, int wr) {
+    k_ncc<<<row_grid((long)W * D, H, 256), 256, 0, s>>>(ref, tar, mref, mtar, cost, D, H, W, hr, wr);
+}
+void launch_combine(cudaStream_t s, float *c1, const float *c2, long n, const float *lut1, const float *lut2,
+                    float lambda1, float lambda2) {
+    long blocks = (n + 255) / 256;
+    if (blocks > 152L * 64) blocks = 152L * 64;
+    k_combine<<<(unsigned)blocks, 256, 0, s>>>(c1, c2, n, lut1, lut2, lambda1, lambda2);
+}
+
+}  // namespace rts

@@ -1,0 +1,127 @@
+// k_wta.cu -- winner-takes-all with the reference's carry semantics, the
+// left/right cross check and small image helpers.
+//
+// seq/WTA.cpp:10-39 declares the winner once per call, so a pixel whose cost
+// has no strictly better d >= 1 than d = 0 keeps the previous pixel's winner
+// (raster order, across rows).  On the GPU this is two passes:
+//   1. k_wta_local: per pixel, the first strict arg-min (arg-max) and whether
+//      any d >= 1 won ("found"); found pixels raise row_last[y] to their x;
+//   2. k_wta_fill: one warp per row takes the incoming winner from the nearest
+//      earlier row that has a found pixel, then propagates within the row with
+//      a ballot scan.
+// raw[p] = found ? 0x100 | winner : 0.  row_last must start at -1.
+#include "rts_common.cuh"
+
+namespace rts {
+
+__global__ void k_wta_local(const float *__restrict__ cost, uint16_t *__restrict__ raw, int *__restrict__ row_last,
+                            int H, int W, int D, int argmax) {
+    const int y = blockIdx.y;
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= W) return;
+    const float *c = cost + ((size_t)y * W + x) * D;
+    float best = c[0];
+    int win = 0;
+    bool found = false;
+    for (int d = 1; d < D; d++) {
+        const float v = c[d];
+        const bool better = argmax ? (v > best) : (v < best);
+        if (better) {
+            best = v;
+            win = d;
+            found = true;
+        }
+    }
+    raw[(size_t)y * W + x] = found ? (uint16_t)(0x100 | win) : (uint16_t)0;
+    if (found) atomicMax(row_last + y, x);
+}
+
+__global__ void k_wta_fill(const uint16_t *__restrict__ raw, const int *__restrict__ row_last,
+                           uint8_t *__restrict__ out, int H, int W, int mirror) {
+    const int lane = threadIdx.x & 31;
+    const int y = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (y >= H) return;
+    // incoming winner: the last found pixel of the nearest earlier row that has one
+    int carry = 0;
+    for (int base = y - 1; base >= 0; base -= 32) {
+        const int yy = base - lane;
+        const bool has = yy >= 0 && row_last[yy] >= 0;
+        const unsigned m = __ballot_sync(0xffffffffu, has);
+        if (m) {
+            const int src = __ffs(m) - 1;  // lowest lane = highest row
+            const int yy0 = base - src;
+            carry = raw[(size_t)yy0 * W + row_last[yy0]] & 0xff;
+            break;
+        }
+    }
+    const uint16_t *r = raw + (size_t)y * W;
+    uint8_t *o = out + (size_t)y * W;
+    for (int x0 = 0; x0 < W; x0 += 32) {
+        const int x = x0 + lane;
+        const uint16_t v = x < W ? r[x] : (uint16_t)0;
+        const unsigned fm = __ballot_sync(0xffffffffu, (v & 0x100) != 0);
+        const unsigned le = fm & (0xffffffffu >> (31 - lane));
+        const int src = le ? 31 - __clz(le) : 0;
+        const int got = __shfl_sync(0xffffffffu, v & 0xff, src);
+        const int val = le ? got : carry;
+        if (x < W) o[mirror ? W - 1 - x : x] = (uint8_t)val;
+        if (fm) carry = __shfl_sync(0xffffffffu, v & 0xff, 31 - __clz(fm));
+    }
+}
+
+// seq/CrossCheck.cpp:10-23
+__global__ void k_cross_check(const uint8_t *__restrict__ dl, const uint8_t *__restrict__ dr,
+                              uint8_t *__restrict__ mask, int H, int W) {
+    const int y = blockIdx.y;
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= W) return;
+    const int v = dl[(size_t)y * W + x];
+    int xt = x - v;
+    if (xt < 0) xt += W;
+    mask[(size_t)y * W + x] = (dr[(size_t)y * W + xt] == v) ? 1 : 0;
+}
+
+// copy with optional horizontal mirror, ch channels per pixel
+__global__ void k_flip(const uint8_t *__restrict__ in, uint8_t *__restrict__ out, int H, int W, int ch, int mirror) {
+    const int y = blockIdx.y;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= W * ch) return;
+    const int x = i / ch, c = i - x * ch;
+    const int xs = mirror ? W - 1 - x : x;
+    out[((size_t)y * W + x) * ch + c] = in[((size_t)y * W + xs) * ch + c];
+}
+
+void launch_wta_local(cudaStream_t s, const float *cost, uint16_t *raw, int *row_last, int H, int W, int D,
+                      int argmax) {
+    k_wta_local<<<dim3((W + 127) / 128, H), 128, 0, s>>>(cost, raw, row_last, H, W, D, argmax);
+}
+void launch_wta_fill(cudaStream_t s, const uint16_t *raw, const int *row_last, uint8_t *out, int H, int W,
+                     int mirror) {
+    k_wta_fill<<<(H + 7) / 8, 256, 0, s>>>(raw, row_last, out, H, W, mirror);
+}
+void launch_cross_check(cudaStream_t s, const uint8_t *dl, const uint8_t *dr, uint8_t *mask, int H, int W) {
+    k_cross_check<<<dim3((W + 127) / 128, H), 128, 0, s>>>(dl, dr, mask, H, W);
+}
+void launch_flip(cudaStream_t s, const uint8_t *in, uint8_t *out, int H, int W, int ch, int mirror) {
+    k_flip<<<dim3((W * ch + 255) / 256, H), 256, 0, s>>>(in, out, H, W, ch, mirror);
+}
+
+}  // namespace rts
+
+namespace rts {
+
+// gray -> RGB by replication (what an 8-bit gray file yields when read as colour)
+__global__ void k_gray_to_rgb(const uint8_t *__restrict__ g, uint8_t *__restrict__ rgb, long n) {
+    const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint8_t v = g[i];
+    rgb[3 * i] = v;
+    rgb[3 * i + 1] = v;
+    rgb[3 * i + 2] = v;
+}
+
+void launch_gray_to_rgb(cudaStream_t s, const uint8_t *g, uint8_t *rgb, long n) {
+    k_gray_to_rgb<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(g, rgb, n);
+}
+
+}  // namespace rts

@@ -1,0 +1,36 @@
+// rts_common.cuh -- device helpers shared by the kernels of rtstereo_gb300.
+#pragma once
+
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "rts_internal.h"
+
+namespace rts {
+
+// Single wrap of an index that is at most one period outside [0, n): the
+// reference's border rule (e.g. seq/CensusTransform.cpp:21-22).
+__device__ __forceinline__ int wrap1(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
+
+// Target column of disparity d: dir > 0 => x-d (+W if negative, L2R,
+// seq/PixelBasedCost.cpp:19-20); dir < 0 => x+d (-W if >= W, R2L, :32-33).
+__device__ __forceinline__ int tar_col(int x, int d, int W, int dir) {
+    if (dir > 0) {
+        int t = x - d;
+        return t < 0 ? t + W : t;
+    }
+    int t = x + d;
+    return t >= W ? t - W : t;
+}
+
+__device__ __forceinline__ int imin(int a, int b) { return a < b ? a : b; }
+__device__ __forceinline__ int imax(int a, int b) { return a > b ? a : b; }
+
+// Packed cross arms of one pixel: left | right<<8 | top<<16 | bottom<<24.
+__device__ __forceinline__ int arm_l(uint32_t a) { return (int)(a & 0xff); }
+__device__ __forceinline__ int arm_r(uint32_t a) { return (int)((a >> 8) & 0xff); }
+__device__ __forceinline__ int arm_t(uint32_t a) { return (int)((a >> 16) & 0xff); }
+__device__ __forceinline__ int arm_b(uint32_t a) { return (int)(a >> 24); }
+
+}  // namespace rts
