@@ -1,0 +1,366 @@
+"""Benchmark of the rtstereo per-frame pipeline on one GB300 (or N replicas).
+
+Default workload (the "plain vs FP16" configuration): one 640x480 random-dot
+stereo pair, D=64, AD+census(9x7) cost combined by CombineCost, adaptive-weight
+aggregation 33x33 (gamma_s 7, gamma_p 36), WTA for the left view and the right
+view (mirrored pipeline), and the left/right cross check.  Metric: MDE/s =
+W*H*D per pair-step (both views) / time.
+
+  value        device-resident inputs, rts_pipeline_run(DEVICE) per step, CUDA events
+               on the launching stream, L2 flushed (256 MB write) before each step
+  e2e          the same call with HOST buffers (pinned): H2D of both images (gray, RGB,
+               Lab) and D2H of both disparity maps and the mask inside the timed step
+  roofline     the dominant kernel (stage timer around its launches, CUDA events)
+  cpu_baseline the CPU oracle on a bounded sample of the same workload
+  --impl reference  the CPU implementation (oracle/_ref if built here, else the oracle
+               port) on all host cores, same metric
+
+Multi-GPU (torchrun, N>1): independent pairs per rank (weak scaling, no collective on
+the data path); the time reported is the max over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    # name: (W, H, D, cost1, cost2, aggr, rects, planes, sigma, seed, extra params)
+    "aw_640x480_d64": (640, 480, 64, 1, 3, 2, 12, 1, 2.0, 0xC1, {}),
+    "cross_384x288_d16": (384, 288, 16, 1, 3, 3, 6, 0, 2.0, 0xC0, {}),
+    "cross_1920x1080_d128": (1920, 1080, 128, 1, 3, 3, 24, 2, 3.0, 0xC2, {}),
+    "cross_1280x720_d128": (1280, 720, 128, 1, 3, 3, 24, 2, 3.0, 0xC2, {}),
+    "aw_1920x1080_d128": (1920, 1080, 128, 1, 3, 2, 24, 2, 3.0, 0xC2, {}),
+    "rank_census_cross_1920x1080_d128": (1920, 1080, 128, 2, 3, 3, 24, 2, 3.0, 0xC2, {"rank_rad": 3}),
+}
+DEFAULT = "aw_640x480_d64"
+
+
+def make_inputs(name):
+    import rtstereo_gb300 as R
+    W, H, D, c1, c2, ag, rects, planes, sigma, seed, extra = WORKLOADS[name]
+    L, Rr, _ = R.synth_pair(seed, W, H, D, rects, planes, sigma, min(4, D - 1))
+    Lc, Rc = R.gray_to_rgb(L), R.gray_to_rgb(Rr)
+    Ll, Rl = R.rgb_to_lab(Lc), R.rgb_to_lab(Rc)
+    return (W, H, D, c1, c2, ag, extra), (L, Rr, Lc, Rc, Ll, Rl)
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "sm_max_mhz": 2070.0}, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_sample(name, rows, threads):
+    """Time the CPU oracle pipeline on `threads` strips of `rows` rows each
+    (independent processes); returns (MDE/s, seconds, sample description)."""
+    import multiprocessing as mp
+    (W, H, D, c1, c2, ag, extra), imgs = make_inputs(name)
+    rows = min(rows, H)
+    strips = []
+    for t in range(threads):
+        y0 = (t * rows) % max(1, H - rows + 1)
+        strips.append(tuple(np.ascontiguousarray(a[y0:y0 + rows]) for a in imgs))
+    ctx = mp.get_context("spawn")
+    t0 = time.perf_counter()
+    with ctx.Pool(threads) as pool:
+        pool.starmap(_cpu_worker, [(name, s) for s in strips])
+    dt = time.perf_counter() - t0
+    mde = threads * W * rows * D / dt / 1e6
+    return mde, dt, f"{threads} x ({W}x{rows} strip, D={D}, full pipeline both views + cross check)"
+
+
+def _cpu_worker(name, strip):
+    import oracle
+    W, H, D, c1, c2, ag, rects, planes, sigma, seed, extra = WORKLOADS[name]
+    L, Rr, Lc, Rc, Ll, Rl = strip
+    kw = dict(extra)
+    if "rank_rad" in kw:
+        kw["rank_rad"] = kw.pop("rank_rad")
+    p = oracle.params(cost1=c1, cost2=c2, aggr=ag, D=D, **kw)
+    oracle.pipeline(p, L, Rr, Lc, Rc, Ll, Rl)
+
+
+def run_reference(args, rank, world):
+    name = args.workload
+    if rank != 0:
+        return
+    import oracle
+    oracle.build()
+    kind = "reference" if oracle.have_reference() else "port"
+    threads = os.cpu_count() or 1
+    rows = args.cpu_rows
+    vals = []
+    for i in range(args.warmup + args.steps):
+        mde, dt, sample = cpu_sample(name, rows, threads)
+        if i >= args.warmup:
+            vals.append((mde, dt))
+    mde = float(np.mean([v[0] for v in vals]))
+    ms = float(np.mean([v[1] for v in vals]) * 1000)
+    W, H, D = WORKLOADS[name][:3]
+    line = {"impl": "reference", "metric": "MDE/s", "value": mde, "unit": "MDE/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic random-dot stereo pair",
+            "config": {"workload": name, "width": W, "height": H, "disp_range": D},
+            "cpu_baseline": {"value": mde, "unit": "MDE/s", "cores": threads, "kind": kind, "sample": sample},
+            "e2e": {"value": mde, "unit": "MDE/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    if kind == "port":
+        line["note"] = "the reference's seq/ sources are not present on this host; the C oracle port is timed"
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, rank, world):
+    import torch
+
+    import rtstereo_gb300 as R
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    name = args.workload
+    (W, H, D, c1, c2, ag, extra), (L, Rr, Lc, Rc, Ll, Rl) = make_inputs(name)
+    prec = R.PREC_F16 if args.precision == "f16" else R.PREC_F32
+    p = R.params(cost1=c1, cost2=c2, aggr=ag, disp_range=D, precision=prec, **extra)
+    ctx = R.Context(dev)
+    # a dedicated (non-default) stream: the library launches on it, the events record on it
+    stream = torch.cuda.Stream(device=dev)
+    torch.cuda.set_stream(stream)
+    ctx.set_stream(stream.cuda_stream)
+
+    # device-resident inputs and outputs
+    t = lambda a: torch.from_numpy(a).to(f"cuda:{dev}")
+    dL, dR, dLc, dRc, dLl, dRl = (t(a) for a in (L, Rr, Lc, Rc, Ll, Rl))
+    o_dl = torch.empty((H, W), dtype=torch.uint8, device=f"cuda:{dev}")
+    o_dr = torch.empty_like(o_dl)
+    o_mk = torch.empty_like(o_dl)
+    pair = R.Pair(W, H, dL.data_ptr(), dR.data_ptr(), dLc.data_ptr(), dRc.data_ptr(), dLl.data_ptr(), dRl.data_ptr())
+    out = R.Out(o_dl.data_ptr(), o_dr.data_ptr(), o_mk.data_ptr(), None)
+    import ctypes as C
+    lib = R.lib()
+
+    def step():
+        ctx.check(lib.rts_pipeline_run(ctx.h, R.DEVICE, C.byref(pair), C.byref(p), C.byref(out)), "pipeline")
+
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{dev}")
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+
+    # timed region: per-step events, L2 flushed before each step (outside the events)
+    ctx.enable_stage_timing(True)
+    ctx.reset_stage_times()
+    launches0 = ctx.kernel_launches
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(dev) as clk:
+        t0 = time.perf_counter()
+        for i in range(args.steps):
+            flush.zero_()
+            evs[i][0].record(stream)
+            step()
+            evs[i][1].record(stream)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    if world > 1:
+        torch.distributed.barrier()
+    launches = ctx.kernel_launches - launches0
+    ms_steps = [a.elapsed_time(b) for a, b in evs]
+    ms = float(np.mean(ms_steps))
+    stages = ctx.stage_times()
+    ctx.enable_stage_timing(False)
+    if world > 1:
+        tt = torch.tensor([ms], device=f"cuda:{dev}")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        ms = float(tt.item())
+    mde_pair = W * H * D / 1e6
+    value = world * mde_pair / (ms / 1e3)
+
+    # e2e: HOST (pinned) buffers through the same public call
+    pin = lambda a: torch.from_numpy(a).pin_memory()
+    hL, hR, hLc, hRc, hLl, hRl = (pin(a) for a in (L, Rr, Lc, Rc, Ll, Rl))
+    ho = [torch.empty((H, W), dtype=torch.uint8).pin_memory() for _ in range(3)]
+    hpair = R.Pair(W, H, hL.data_ptr(), hR.data_ptr(), hLc.data_ptr(), hRc.data_ptr(), hLl.data_ptr(), hRl.data_ptr())
+    hout = R.Out(ho[0].data_ptr(), ho[1].data_ptr(), ho[2].data_ptr(), None)
+
+    def hstep():
+        ctx.check(lib.rts_pipeline_run(ctx.h, R.HOST, C.byref(hpair), C.byref(p), C.byref(hout)), "pipeline")
+
+    for _ in range(max(1, args.warmup)):
+        hstep()
+    e_ms = []
+    for i in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        hstep()
+        e_ms.append((time.perf_counter() - t1) * 1e3)
+    e2e_ms = float(np.mean(e_ms))
+    if world > 1:
+        tt = torch.tensor([e2e_ms], device=f"cuda:{dev}")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        e2e_ms = float(tt.item())
+    h2d = sum(a.numel() for a in (hL, hR, hLc, hRc, hLl, hRl))
+    d2h = 3 * W * H
+
+    # parity spot check of this run's output against the last device run
+    agree = bool(np.array_equal(ho[0].numpy(), o_dl.cpu().numpy()))
+
+    if rank != 0:
+        if world > 1:
+            torch.distributed.destroy_process_group()
+        return
+
+    peaks, src = measured_peaks()
+    roof = roofline(stages, name, W, H, D, ag, peaks, src, p)
+    line = {"metric": "MDE/s", "value": value, "unit": "MDE/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f16" if prec else "f32",
+            "data": "synthetic random-dot stereo pair (seeded, no dataset)",
+            "config": {"workload": name, "width": W, "height": H, "disp_range": D,
+                       "pipeline": "cost1=%d cost2=%d aggr=%d, both views + cross check" % (c1, c2, ag),
+                       "precision": args.precision, "l2": "flushed (256 MB write) before every timed step",
+                       "parallelism": f"replicas{world}"},
+            "e2e": {"value": world * mde_pair / (e2e_ms / 1e3), "unit": "MDE/s", "ms_per_step": e2e_ms,
+                    "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "host_equals_device_result": agree},
+            "gpu_launches": launches, "wall_s": wall,
+            "stages_ms_per_step": {k: v[1] / args.steps for k, v in stages.items()},
+            "roofline": roof, "clocks": clk.summary()}
+    if not args.no_cpu:
+        threads = 1
+        mde, dt, sample = cpu_sample(name, args.cpu_rows, threads)
+        import oracle
+        line["cpu_baseline"] = {"value": mde, "unit": "MDE/s", "cores": threads,
+                                "kind": "reference" if oracle.have_reference() else "port", "sample": sample,
+                                "seconds": dt}
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def roofline(stages, name, W, H, D, ag, peaks, src, p):
+    """Dominant kernel and its algorithmic throughput."""
+    if not stages:
+        return None
+    dom = max(stages.items(), key=lambda kv: kv[1][1])
+    kname, (launches, total_ms) = dom
+    per_launch_ms = total_ms / max(1, launches)
+    E = W * H * D  # entries per view; each launch covers one view
+    if kname == "aw_wta":
+        taps = (2 * p.aw_rad + 1) ** 2
+        flops = 4.0 * taps * E  # w = wR*wT, sum w, C*w, sum: 4 per tap per entry
+        achieved = flops / (per_launch_ms / 1e3) / 1e12
+        mhz = peaks.get("sm_max_mhz", 2070.0)
+        peak = 152 * 128 * 2 * mhz * 1e6 / 1e12  # FFMA lanes x 2 FLOP x clock
+        return {"bound": "fp32", "kernel": "k_aw_wta", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                "frac": achieved / peak, "traffic": None, "launches": launches, "ms_per_launch": per_launch_ms,
+                "flop_per_launch": flops,
+                "peak_source": f"FP32 FMA pipe: 152 SMs x 128 lanes x 2 FLOP x {mhz:.0f} MHz ({src} max clock); "
+                               "the plain form issues 4 unfused FP32 ops per tap, so 0.5 of this is its ceiling"}
+    # HBM-bound stages: compulsory bytes of the launch
+    S = 2 if p.precision else 4
+    if kname == "cross_hseg":
+        byts = S * E + 2 * 16 * W * H
+    elif kname == "cross_vert_wta":
+        byts = S * E + 2 * 16 * W * H + 2 * W * H
+    elif kname == "cost":
+        byts = S * E + 2 * 16 * W * H
+    else:
+        byts = S * E
+    achieved = byts / (per_launch_ms / 1e3) / 1e9
+    peak = peaks["hbm_gbs"]
+    return {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "traffic": None, "launches": launches, "ms_per_launch": per_launch_ms,
+            "bytes_per_launch": byts, "peak_source": src}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default=DEFAULT, choices=sorted(WORKLOADS))
+    ap.add_argument("--precision", default="f32", choices=["f32", "f16"])
+    ap.add_argument("--cpu-rows", type=int, default=None,
+                    help="rows per CPU strip (default 48 for the 1-thread baseline, 24 for --impl reference)")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.cpu_rows is None:
+        args.cpu_rows = 24 if args.impl == "reference" else 48
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_ours(args, rank, world)
+
+
+if __name__ == "__main__":
+    main()

@@ -87,7 +87,7 @@ __global__ void k_cross_aggr(const float *__restrict__ pre, float *__restrict__ 
         int xl = x - l - 1, xrr = x + r;
         if (xl < 0) xl = 0;  // :153-156 the clamped pixel is excluded from the sum, still counted
         else if (xrr >= W) xrr = W - 1;
-        if (xl >= 0 && xrr < W) {  // :157, always true for arms made by findCross
+        if (xl >= 0 && xrr < W && xl < W && xrr >= 0) {  // :157, always true for arms made by findCross
             const float *row = pre + (size_t)yy * W * D + d;
             sum = __fadd_rn(sum, __fsub_rn(row[(size_t)xrr * D], row[(size_t)xl * D]));
             cnt += r + l + 1;
@@ -183,8 +183,10 @@ __global__ void k_disp_refine(const uint8_t *__restrict__ in, uint8_t *__restric
         if (yy < 0 || yy >= H) continue;
         const long pr = (long)yy * W + x;
         int xl = x - horz[2 * pr], xr = x + horz[2 * pr + 1];
-        if (xl < 0) xl = 0;
-        else if (xr >= W) xr = W - 1;
+        // the reference clamps one side (:189-192); arms made by findCross never
+        // reach past either edge, so clamping both only guards foreign input
+        xl = imax(xl, 0);
+        xr = imin(xr, W - 1);
         for (int xx = xl; xx <= xr; xx++) hist[in[(size_t)yy * W + xx]]++;
     }
     int best = hist[0], arg = 0;

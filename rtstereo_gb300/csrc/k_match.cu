@@ -202,14 +202,6 @@ __global__ void k_ncc(const uint8_t *__restrict__ ref, const uint8_t *__restrict
     if (den != 0.f) cost[((size_t)y * W + x) * D + d] = __fdiv_rn(nom, den);
 }
 
-// CombineCost (seq/CombineCost.cpp:11-25).  Integer-valued costs in range take
-// 1-expf(-v/lambda) from a table computed on the host with the C library's
-// expf (the reference's arithmetic); other values use the device expf.
-__device__ __forceinline__ float combine_term(float v, const float *__restrict__ lut, float lambda) {
-    if (v >= 0.f && v < (float)kCombineLut && v == truncf(v)) return lut[(int)v];
-    return __fsub_rn(1.0f, expf(__fdiv_rn(-v, lambda)));
-}
-
 __global__ void k_combine(float *__restrict__ c1, const float *__restrict__ c2, long n, const float *__restrict__ lut1,
                           const float *__restrict__ lut2, float lambda1, float lambda2) {
     for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {

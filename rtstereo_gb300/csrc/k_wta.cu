@@ -77,7 +77,8 @@ __global__ void k_cross_check(const uint8_t *__restrict__ dl, const uint8_t *__r
     if (x >= W) return;
     const int v = dl[(size_t)y * W + x];
     int xt = x - v;
-    if (xt < 0) xt += W;
+    if (xt < 0) xt += W;        // seq/CrossCheck.cpp:16
+    if (xt < 0) xt = ((xt % W) + W) % W;  // only for disparities above the width
     mask[(size_t)y * W + x] = (dr[(size_t)y * W + xt] == v) ? 1 : 0;
 }
 

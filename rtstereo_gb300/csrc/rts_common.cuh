@@ -33,4 +33,13 @@ __device__ __forceinline__ int arm_r(uint32_t a) { return (int)((a >> 8) & 0xff)
 __device__ __forceinline__ int arm_t(uint32_t a) { return (int)((a >> 16) & 0xff); }
 __device__ __forceinline__ int arm_b(uint32_t a) { return (int)(a >> 24); }
 
+// One term of CombineCost (seq/CombineCost.cpp:21-22): 1 - exp(-v/lambda).
+// Integer-valued costs in range take it from a table computed on the host with
+// the C library's expf (the reference's arithmetic, so bit-identical); other
+// values use the device expf (within a few ulp).
+__device__ __forceinline__ float combine_term(float v, const float *__restrict__ lut, float lambda) {
+    if (v >= 0.f && v < (float)kCombineLut && v == truncf(v)) return lut[(int)v];
+    return __fsub_rn(1.0f, expf(__fdiv_rn(-v, lambda)));
+}
+
 }  // namespace rts

@@ -31,7 +31,7 @@ enum Slot {
     SL_V_CODES, SL_V_ARMS, SL_V_AUX,        // census codes, packed arms, rank/LoG images
     SL_V_COST1, SL_V_COST2, SL_V_SEG,       // cost volumes / horizontal segment sums
     SL_V_RAW, SL_V_ROWLAST, SL_V_DISP,      // WTA winners, row summaries, view disparities
-    SL_V_MEAN,
+    SL_V_MEAN, SL_V_REC,                    // NCC means, fused-path pixel records
     SL_BATCH0, SL_BATCH1, SL_BATCH2, SL_BATCH3,
     SL_COUNT
 };

@@ -6,14 +6,22 @@
 
 namespace rts {
 
-// True when view_fused handles this configuration (otherwise the composed
-// module-kernel path runs).
+// AD / census (<= 64-bit window) single or combined costs, computed on the fly
+bool fast_costs(const rts_params &p);
+// cross-based (arm <= 23) and adaptive-weight (radius <= 16) aggregation
 bool fused_supported(const rts_params &p, int H, int W);
 
-// One view of the pipeline with fused kernels; all pointers are device memory.
-// disp receives the view's disparities, mirrored in x when `mirror` is set.
-rts_status view_fused(rts_ctx *c, const rts_params &p, int H, int W, const uint8_t *gref, const uint8_t *gtar,
-                      const uint8_t *cref, const uint8_t *ctar, const uint8_t *lref, const uint8_t *ltar,
-                      uint8_t *disp, int mirror);
+// 16-byte per-pixel records: census code, packed RGB, packed cross arms
+rts_status prep_records(rts_ctx *c, const rts_params &p, int H, int W, const uint8_t *gray, const uint8_t *rgb,
+                        uint4 *rec, uint32_t *arms_out);
+// cost volume [H][W][D] (float, or __half when half != 0) from records
+rts_status cost_volume_fast(rts_ctx *c, const rts_params &p, int H, int W, const uint4 *rr, const uint4 *rt,
+                            void *vol, int half);
+// cross-based aggregation + arg-min; vol == nullptr computes the cost on the fly
+rts_status cross_fused(rts_ctx *c, const rts_params &p, int H, int W, const uint4 *rr, const uint4 *rt,
+                       const uint32_t *ar, const uint32_t *at, const float *vol, uint16_t *raw, int *row_last);
+// adaptive-weight aggregation + arg-min over a float (half == 0) or __half volume
+rts_status aw_fused(rts_ctx *c, const rts_params &p, int H, int W, const void *vol, int half, const uint8_t *labr,
+                    const uint8_t *labt, uint16_t *raw, int *row_last, float *cost_out);
 
 }  // namespace rts

@@ -192,10 +192,67 @@ static rts_status view_composed(rts_ctx *c, const rts_params &p, int H, int W, c
     return check_launch(c, "pipeline view");
 }
 
+// Fused path for one view (cross-based or adaptive-weight aggregation).
+static rts_status view_fused(rts_ctx *c, const rts_params &p, int H, int W, const ViewIn &v, uint8_t *disp,
+                             int mirror) {
+    const int D = p.disp_range;
+    const size_t np = (size_t)H * W, ne = np * D;
+    cudaStream_t s = c->stream;
+    const bool half = p.precision == RTS_PREC_F16;
+    void *recv, *raw, *rl;
+    RTS_TRY(scratch(c, SL_V_REC, np * 40, &recv));
+    uint4 *rr = (uint4 *)recv, *rt = rr + np;
+    uint32_t *ar = (uint32_t *)(rt + np), *at = ar + np;  // compact arms
+    RTS_TRY(scratch(c, SL_V_RAW, np * 2, &raw));
+    RTS_TRY(scratch(c, SL_V_ROWLAST, (size_t)H * 4, &rl));
+    RTS_CU(c, cudaMemsetAsync(rl, 0xff, (size_t)H * 4, s));
+    {
+        StageScope sc(c, "prep");
+        const bool cross = p.aggr == RTS_AGGR_CROSS;
+        RTS_TRY(prep_records(c, p, H, W, v.gref, v.cref, rr, cross ? ar : nullptr));
+        RTS_TRY(prep_records(c, p, H, W, v.gtar, v.ctar, rt, cross ? at : nullptr));
+    }
+    const bool fast = fast_costs(p);
+    const void *vol = nullptr;
+    int vol_half = 0;
+    if (!fast || p.aggr == RTS_AGGR_AW) {
+        StageScope sc(c, "cost");
+        void *c1v;
+        if (fast) {
+            vol_half = half ? 1 : 0;
+            RTS_TRY(scratch(c, SL_V_COST1, ne * (half ? 2 : 4), &c1v));
+            RTS_TRY(cost_volume_fast(c, p, H, W, rr, rt, c1v, vol_half));
+        } else {
+            RTS_TRY(scratch(c, SL_V_COST1, ne * 4, &c1v));
+            RTS_TRY(one_cost(c, p, p.cost1, p.aggr == RTS_AGGR_CROSS, H, W, v, (float *)c1v, SL_V_AUX));
+            if (p.cost2 != RTS_COST_NONE) {
+                void *c2v;
+                RTS_TRY(scratch(c, SL_V_COST2, ne * 4, &c2v));
+                RTS_TRY(one_cost(c, p, p.cost2, false, H, W, v, (float *)c2v, SL_TMP2));
+                const float *l1, *l2;
+                RTS_TRY(combine_luts(c, p.lambda1, p.lambda2, &l1, &l2));
+                launch_combine(s, (float *)c1v, (const float *)c2v, (long)ne, l1, l2, p.lambda1, p.lambda2);
+                count_launch(c);
+            }
+        }
+        vol = c1v;
+    }
+    if (p.aggr == RTS_AGGR_CROSS) {
+        RTS_TRY(cross_fused(c, p, H, W, rr, rt, ar, at, (const float *)vol, (uint16_t *)raw, (int *)rl));
+    } else {
+        RTS_TRY(aw_fused(c, p, H, W, vol, vol_half, v.lref, v.ltar, (uint16_t *)raw, (int *)rl, nullptr));
+    }
+    {
+        StageScope sc(c, "wta_fill");
+        launch_wta_fill(s, (const uint16_t *)raw, (const int *)rl, disp, H, W, mirror);
+        count_launch(c);
+    }
+    return check_launch(c, "pipeline view");
+}
+
 rts_status run_view(rts_ctx *c, const rts_params &p, int H, int W, const ViewIn &v, uint8_t *disp, int mirror,
                     float *cost_out) {
-    if (!cost_out && fused_supported(p, H, W)) return view_fused(c, p, H, W, v.gref, v.gtar, v.cref, v.ctar, v.lref,
-                                                                 v.ltar, disp, mirror);
+    if (!cost_out && fused_supported(p, H, W)) return view_fused(c, p, H, W, v, disp, mirror);
     return view_composed(c, p, H, W, v, disp, mirror, cost_out);
 }
 
@@ -206,7 +263,8 @@ rts_status pipeline_device(rts_ctx *c, const rts_params &p, int H, int W, const 
     const size_t np = (size_t)H * W;
     cudaStream_t s = c->stream;
     const bool need_lab = p.aggr == RTS_AGGR_AW;
-    const bool need_rgb = p.cost1 == RTS_COST_AD || p.cost2 == RTS_COST_AD || p.aggr == RTS_AGGR_CROSS;
+    // the fused kernels read packed colour records even for gray-only costs
+    const bool need_rgb = true;
     void *rgbv = nullptr;
     if (need_rgb && (!lc || !rc)) {
         // gray replicated into three channels (seq/Main.cpp:87-90 reads the files as colour)

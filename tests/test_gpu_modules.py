@@ -142,7 +142,8 @@ def test_device_pointers_and_stream(ctx, oracle_mod):
     L, Rr, Lc, Rc = images(7, H, W)
     dl, dr = torch.from_numpy(Lc).cuda(), torch.from_numpy(Rc).cuda()
     out = torch.empty((H, W, D), dtype=torch.float32, device="cuda")
-    s = torch.cuda.current_stream()
+    s = torch.cuda.Stream()  # a real stream handle (the legacy default stream is handle 0)
+    s.wait_stream(torch.cuda.current_stream())
     ctx.set_stream(s.cuda_stream)
     try:
         ctx.call("pixelBasedCostL2R_Color_trunc", R.DEVICE, dl, dr, out, D, H, W, C.c_float(24.0), 0)

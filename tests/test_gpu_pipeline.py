@@ -82,6 +82,8 @@ def test_adaptive_weight_pipeline(ctx, oracle_mod, W, H, D, rad):
 def test_fused_paths_match_oracle(ctx, oracle_mod):
     # no cost output requested: the fused kernels run where they exist
     for kw in (dict(disp_range=16, aggr=3), dict(disp_range=64, aggr=3), dict(disp_range=32, aggr=2, aw_rad=7),
+               dict(disp_range=80, aggr=2, aw_rad=16), dict(disp_range=100, aggr=3, cost1=3, cost2=1),
+               dict(disp_range=40, aggr=3, cost1=2, cost2=3, rank_rad=2), dict(disp_range=24, aggr=2, cost1=3, cost2=0),
                dict(disp_range=24, aggr=1, box_rad=4), dict(disp_range=48, aggr=0)):
         L, Rr = synth(kw["disp_range"], 160, 50, kw["disp_range"], 5, 1)
         g, o = run_both(ctx, oracle_mod, L, Rr, **kw)
@@ -132,3 +134,16 @@ def test_golden_modules(ctx, golden):
         wl = ctx.computeWeights(pw, golden["aw/labL"], 7.0, rad)
         wr = ctx.computeWeights(pw, golden["aw/labR"], 7.0, rad)
         assert bits_equal(ctx.calcAWCostL2R(wl, wr, golden["aw/cost"], rad), golden[f"aw{rad}/l2r"])
+
+
+@pytest.mark.parametrize("kw", [dict(disp_range=64, aggr=3), dict(disp_range=48, aggr=2, aw_rad=16)])
+def test_fp16_form_agrees_with_plain(ctx, kw):
+    """FP16 storage (fp32 accumulation): most disparities equal the plain form's."""
+    import rtstereo_gb300 as R
+    L, Rr = synth(kw["disp_range"] + 1, 200, 60, kw["disp_range"], 6, 1)
+    Lc, Rc = R.gray_to_rgb(L), R.gray_to_rgb(Rr)
+    lab = (R.rgb_to_lab(Lc), R.rgb_to_lab(Rc))
+    a = ctx.pipeline(R.params(precision=R.PREC_F32, **kw), L, Rr, Lc, Rc, *lab)
+    b = ctx.pipeline(R.params(precision=R.PREC_F16, **kw), L, Rr, Lc, Rc, *lab)
+    agree = (a[0] == b[0]).mean()
+    assert agree > 0.97, agree
