@@ -152,6 +152,17 @@ rts_status rts_calcAWCostR2L(rts_ctx *, rts_mem, const float *weightRef, const f
 rts_status rts_WTA(rts_ctx *, rts_mem, const float *cost, uint8_t *winners, int rdim, int cdim, int dispRange);
 /* seq/WTA.cpp:26-39 */
 rts_status rts_WTA_NCC(rts_ctx *, rts_mem, const float *cost, uint8_t *winners, int rdim, int cdim, int dispRange);
+/* No counterpart in the reference.  rts_WTA for callers that cannot allocate
+ * device memory (a host that fixes its device memory at start-up, or a frame
+ * loop that must not hit the device-wide synchronisation of cudaMalloc/cudaFree).
+ * DEVICE pointers only, enqueued on cuda_stream (NULL: the legacy default
+ * stream); no context.  Its scratch is a static device array built into the
+ * library (about 4 MiB, held by every GPU that loads the library until exit):
+ * rdim*cdim <= 2,097,152 and rdim <= 8192, else RTS_ERR_INVALID_ARG.  The first
+ * call on a device looks up that array's device address with the device current,
+ * so make it before any stream capture.  All calls share the array: calls whose
+ * work overlaps on the GPU race and must be serialised by the caller. */
+rts_status rts_WTA_noalloc(const float *cost, uint8_t *winners, int rdim, int cdim, int dispRange, void *cuda_stream);
 /* seq/CrossCheck.cpp:10-23 */
 rts_status rts_cross_check(rts_ctx *, rts_mem, const uint8_t *ref_disparity, const uint8_t *tar_disparity,
                            uint8_t *cross_check_image, int rdim, int cdim);

@@ -94,6 +94,7 @@ SIGNATURES = {
     "rts_WTA": (i, [p, i, p, p, i, i, i]),
     "rts_WTA_NCC": (i, [p, i, p, p, i, i, i]),
     "rts_cross_check": (i, [p, i, p, p, p, i, i]),
+    "rts_WTA_noalloc": (i, [p, p, i, i, i, p]),
     "rts_params_default": (None, [C.POINTER(Params)]),
     "rts_pipeline_run": (i, [p, i, C.POINTER(Pair), C.POINTER(Params), C.POINTER(Out)]),
     "rts_batch_run": (i, [p, i, C.POINTER(Pair), C.POINTER(Params), C.POINTER(Out)]),
