@@ -173,6 +173,138 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+MIX_SIZES = [(320, 240), (640, 480), (1024, 768), (1280, 720), (1920, 1080)]
+MIX_DISP = [32, 64, 128]
+
+
+def mixed_pairs(n, seed0):
+    """n random-dot pairs with sizes and disparity ranges drawn from the mixed set."""
+    import rtstereo_gb300 as R
+    rng = np.random.default_rng(seed0)
+    out = []
+    for i in range(n):
+        W, H = MIX_SIZES[rng.integers(len(MIX_SIZES))]
+        D = MIX_DISP[rng.integers(len(MIX_DISP))]
+        L, Rr, _ = R.synth_pair(seed0 + i, W, H, D, 6, 0, 2.0, 4)
+        out.append((L, Rr, D))
+    return out
+
+
+def run_batch(args, rank, world):
+    """64 mixed pairs through rts_batch_run (one launch per stage, CUDA graph)."""
+    import ctypes as C
+
+    import torch
+
+    import rtstereo_gb300 as R
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    prec = R.PREC_F16 if args.precision == "f16" else R.PREC_F32
+    data = mixed_pairs(args.pairs, 0xC3000 + 1000 * rank)
+    ctx = R.Context(dev)
+    stream = torch.cuda.Stream(device=dev)
+    torch.cuda.set_stream(stream)
+    ctx.set_stream(stream.cuda_stream)
+    keep, pairs, params, outs = [], [], [], []
+    mde = 0.0
+    for L, Rr, D in data:
+        H, W = L.shape
+        dl, dr = torch.from_numpy(L).cuda(), torch.from_numpy(Rr).cuda()
+        o = [torch.empty((H, W), dtype=torch.uint8, device="cuda") for _ in range(3)]
+        keep += [dl, dr] + o
+        pairs.append(R.Pair(W, H, dl.data_ptr(), dr.data_ptr(), None, None, None, None))
+        params.append(R.params(disp_range=D, precision=prec))
+        outs.append(R.Out(o[0].data_ptr(), o[1].data_ptr(), o[2].data_ptr(), None))
+        mde += W * H * D / 1e6
+    for _ in range(args.warmup):  # the first call autotunes and captures the graph
+        ctx.batch_run(pairs, params, outs)
+    torch.cuda.synchronize()
+    launches0 = ctx.kernel_launches
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    with ClockSampler(dev) as clk:
+        for i in range(args.steps):
+            flush.zero_()
+            evs[i][0].record(stream)
+            ctx.batch_run(pairs, params, outs)
+            evs[i][1].record(stream)
+        torch.cuda.synchronize()
+    ms = float(np.mean([a.elapsed_time(b) for a, b in evs]))
+    # the plain path for comparison: the same pairs one pipeline run at a time
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    lib = R.lib()
+    for _ in range(2):  # warm-up: each shape is tuned and captured on its first run
+        for pr, pp, po in zip(pairs, params, outs):
+            ctx.check(lib.rts_pipeline_run(ctx.h, R.DEVICE, C.byref(pr), C.byref(pp), C.byref(po)), "pipeline")
+    torch.cuda.synchronize()
+    t0.record(stream)
+    for pr, pp, po in zip(pairs, params, outs):
+        ctx.check(lib.rts_pipeline_run(ctx.h, R.DEVICE, C.byref(pr), C.byref(pp), C.byref(po)), "pipeline")
+    t1.record(stream)
+    torch.cuda.synchronize()
+    ms_plain = t0.elapsed_time(t1)
+    line = {"metric": "MDE/s", "value": mde / (ms / 1e3), "unit": "MDE/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": args.precision, "data": "synthetic random-dot stereo pairs (seeded)",
+            "config": {"workload": "batch_mixed", "pairs": args.pairs, "sizes": MIX_SIZES, "disp": MIX_DISP,
+                       "pipeline": "AD+census, cross-based, both views + cross check", "form": "rts_batch_run (graph)"},
+            "one_pair_at_a_time_ms": ms_plain, "batch_speedup_vs_one_at_a_time": ms_plain / ms,
+            "gpu_launches": ctx.kernel_launches - launches0, "clocks": clk.summary()}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def run_serve(args, rank, world):
+    """Poisson request stream through rts_server_* (continuous batching)."""
+    import rtstereo_gb300 as R
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    import torch
+    torch.cuda.set_device(dev)
+    prec = R.PREC_F16 if args.precision == "f16" else R.PREC_F32
+    pool = mixed_pairs(32, 0xC4000)
+    rng = np.random.default_rng(0xC4)
+    n = args.requests
+    arrivals = np.cumsum(rng.exponential(1.0 / args.rate, n))
+    choice = rng.integers(len(pool), size=n)
+    ctx = R.Context(dev)
+    srv = R.Server(ctx, hbm_budget=int(args.budget_gb * (1 << 30)), max_inflight=64, max_batch=args.max_batch,
+                   precision=prec)
+    # warm up the kernels on each size once
+    for L, Rr, D in pool[:4]:
+        srv.wait(srv.submit(R.params(disp_range=D, precision=prec), L, Rr)[0])
+    tickets = []
+    t0 = time.perf_counter()
+    i = 0
+    mde = 0.0
+    while i < n:
+        now = time.perf_counter() - t0
+        while i < n and arrivals[i] <= now:
+            L, Rr, D = pool[choice[i]]
+            tickets.append(srv.submit(R.params(disp_range=D, precision=prec), L, Rr)[0])
+            mde += L.shape[0] * L.shape[1] * D / 1e6
+            i += 1
+        srv.progress()
+    lat = []
+    for t in tickets:
+        sub, start, done = srv.wait(t)
+        lat.append(done - sub)
+    wall = time.perf_counter() - t0
+    srv.close()
+    lat = np.array(lat)
+    line = {"metric": "pairs/s", "value": n / wall, "unit": "pairs/s", "n_gpus": world, "steps": n, "warmup": 4,
+            "ms_per_step": wall * 1e3 / n, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": args.precision, "data": "synthetic random-dot stereo pairs (seeded)",
+            "config": {"workload": "serve_poisson", "requests": n, "rate_per_s": args.rate,
+                       "hbm_budget_gb": args.budget_gb, "max_batch": args.max_batch, "sizes": MIX_SIZES,
+                       "disp": MIX_DISP},
+            "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
+                           "max": float(lat.max())},
+            "MDE_per_s": mde / wall}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def run_ours(args, rank, world):
     import torch
 
@@ -212,8 +344,6 @@ def run_ours(args, rank, world):
     torch.cuda.synchronize()
 
     # timed region: per-step events, L2 flushed before each step (outside the events)
-    ctx.enable_stage_timing(True)
-    ctx.reset_stage_times()
     launches0 = ctx.kernel_launches
     evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     if world > 1:
@@ -233,6 +363,14 @@ def run_ours(args, rank, world):
     launches = ctx.kernel_launches - launches0
     ms_steps = [a.elapsed_time(b) for a, b in evs]
     ms = float(np.mean(ms_steps))
+    # per-kernel times from the library's stage timer (CUDA events around every
+    # launch on the launching stream), on extra steps outside the timed region
+    ctx.enable_stage_timing(True)
+    ctx.reset_stage_times()
+    for i in range(args.steps):
+        flush.zero_()
+        step()
+    torch.cuda.synchronize()
     stages = ctx.stage_times()
     ctx.enable_stage_timing(False)
     if world > 1:
@@ -346,7 +484,12 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default=DEFAULT, choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default=DEFAULT, choices=sorted(WORKLOADS) + ["batch_mixed", "serve_poisson"])
+    ap.add_argument("--pairs", type=int, default=64, help="batch_mixed: pairs per batch")
+    ap.add_argument("--requests", type=int, default=2000, help="serve_poisson: requests in the stream")
+    ap.add_argument("--rate", type=float, default=2000.0, help="serve_poisson: Poisson arrival rate (pairs/s)")
+    ap.add_argument("--budget-gb", type=float, default=40.0, help="serve_poisson: HBM admitted at once")
+    ap.add_argument("--max-batch", type=int, default=8, help="serve_poisson: pairs launched together")
     ap.add_argument("--precision", default="f32", choices=["f32", "f16"])
     ap.add_argument("--cpu-rows", type=int, default=None,
                     help="rows per CPU strip (default 48 for the 1-thread baseline, 24 for --impl reference)")
@@ -358,6 +501,10 @@ def main():
     rank = int(os.environ.get("RANK", "0"))
     if args.impl == "reference":
         run_reference(args, rank, world)
+    elif args.workload == "batch_mixed":
+        run_batch(args, rank, world)
+    elif args.workload == "serve_poisson":
+        run_serve(args, rank, world)
     else:
         run_ours(args, rank, world)
 

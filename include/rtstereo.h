@@ -218,6 +218,37 @@ rts_status rts_pipeline_run(rts_ctx *, rts_mem, const rts_pair *pair, const rts_
  * batch shape. */
 rts_status rts_batch_run(rts_ctx *, int n, const rts_pair *pairs, const rts_params *params, rts_out *outs);
 
+/* ---- serving loop (continuous batching) -------------------------------------- */
+/* Requests (HOST buffers, copied on submit) are admitted in arrival order while
+ * a slot and enough of the server's device pool are free, launched as batches
+ * on a ring of streams (a batch overlaps with the ones still running) and
+ * completed by polling.  All requests of a server share every parameter except
+ * disp_range; the pipeline is the fused cross-based one. */
+typedef struct rts_server rts_server;
+typedef struct rts_server_config {
+    size_t hbm_budget;   /* bytes of cost-volume memory admitted at once (e.g. 40 GB) */
+    int max_inflight;    /* slots: pairs on the device at once */
+    int max_batch;       /* pairs launched together */
+    int precision;       /* RTS_PREC_F32 or RTS_PREC_F16 */
+} rts_server_config;
+
+typedef struct rts_request_stats {
+    double submit_ms, start_ms, done_ms; /* host clock, ms since server creation */
+} rts_request_stats;
+
+rts_status rts_server_create(rts_server **out, rts_ctx *ctx, const rts_server_config *cfg);
+void rts_server_destroy(rts_server *s);
+/* Copies the HOST inputs (pair) on submit; outputs land in HOST out buffers. */
+rts_status rts_server_submit(rts_server *s, const rts_pair *pair, const rts_params *params, rts_out *out,
+                             uint64_t *ticket);
+/* 1 done, 0 pending, <0 an error status (negated) */
+int rts_server_poll(rts_server *s, uint64_t ticket);
+rts_status rts_server_wait(rts_server *s, uint64_t ticket, double timeout_ms, rts_request_stats *stats);
+rts_status rts_server_cancel(rts_server *s, uint64_t ticket);
+/* Drives admission and completion; call from the submitting thread or let
+ * rts_server_wait drive it. */
+rts_status rts_server_progress(rts_server *s);
+
 /* ---- synthetic random-dot stereo pairs (host) ------------------------------ */
 /* Left: uniform u8 texture smoothed by a 3x3 box ((sum+4)/9, clamp-to-edge).
  * Right(y,x) = Left(y, clamp(x + d(y,x))) + N(0, sigma), rounded half away and

@@ -16,9 +16,10 @@ import numpy as np
 
 from . import _native as N
 from ._native import (AGGR_AW, AGGR_BOX, AGGR_CROSS, AGGR_NONE, COST_AD, COST_CENSUS, COST_LOG, COST_NCC,
-                      COST_NONE, COST_RANK, DEVICE, HOST, PREC_F16, PREC_F32, Out, Pair, Params, RtsError)
+                      COST_NONE, COST_RANK, DEVICE, HOST, PREC_F16, PREC_F32, Out, Pair, Params, RequestStats,
+                      RtsError, ServerConfig)
 
-__all__ = ["Context", "Params", "Pair", "Out", "RtsError", "params", "synth_pair", "gray_to_rgb", "rgb_to_lab",
+__all__ = ["Context", "Server", "Params", "Pair", "Out", "RtsError", "params", "synth_pair", "gray_to_rgb", "rgb_to_lab",
            "HOST", "DEVICE", "COST_NONE", "COST_AD", "COST_RANK", "COST_CENSUS", "COST_LOG", "COST_NCC",
            "AGGR_NONE", "AGGR_BOX", "AGGR_AW", "AGGR_CROSS", "PREC_F32", "PREC_F16", "lib"]
 
@@ -316,3 +317,66 @@ class Context:
         out = Out(_ptr(dl), _ptr(dr), _ptr(mk), _ptr(cost))
         self.check(self._lib.rts_pipeline_run(self.h, HOST, C.byref(pair), C.byref(p), C.byref(out)), "pipeline")
         return dl, dr, mk, cost
+
+    # -- batched form (DEVICE buffers) ---------------------------------------------
+    def batch_run(self, pairs, params, outs):
+        """rts_batch_run over lists of Pair / Params / Out holding DEVICE pointers."""
+        n = len(pairs)
+        PA, PR, PO = (Pair * n)(*pairs), (Params * n)(*params), (Out * n)(*outs)
+        self.check(self._lib.rts_batch_run(self.h, n, PA, PR, PO), "batch_run")
+
+
+class Server:
+    """rts_server: continuous-batching request loop over one context."""
+
+    def __init__(self, ctx: Context, hbm_budget: int, max_inflight: int = 64, max_batch: int = 16,
+                 precision: int = PREC_F16):
+        self.ctx = ctx
+        self._lib = ctx._lib
+        h = C.c_void_p()
+        cfg = ServerConfig(hbm_budget, max_inflight, max_batch, precision)
+        ctx.check(self._lib.rts_server_create(C.byref(h), ctx.h, C.byref(cfg)), "server_create")
+        self.h = h
+        self._keep = {}
+
+    def close(self):
+        if getattr(self, "h", None):
+            self._lib.rts_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def submit(self, p: Params, lgray, rgray, lrgb=None, rrgb=None):
+        """Queues a pair (HOST arrays, copied now); returns (ticket, (disp_l, disp_r, mask))."""
+        H, W = lgray.shape
+        pair = Pair(W, H, _ptr(lgray), _ptr(rgray), _ptr(lrgb), _ptr(rrgb), None, None)
+        outs = tuple(np.zeros((H, W), np.uint8) for _ in range(3))
+        out = Out(_ptr(outs[0]), _ptr(outs[1]), _ptr(outs[2]), None)
+        t = C.c_uint64()
+        st = self._lib.rts_server_submit(self.h, C.byref(pair), C.byref(p), C.byref(out), C.byref(t))
+        if st != 0:
+            raise RtsError(st, self._lib.rts_ctx_last_error(self.ctx.h).decode(errors="replace"))
+        self._keep[t.value] = outs
+        return t.value, outs
+
+    def progress(self):
+        self.ctx.check(self._lib.rts_server_progress(self.h), "server_progress")
+
+    def poll(self, ticket) -> int:
+        return int(self._lib.rts_server_poll(self.h, ticket))
+
+    def cancel(self, ticket) -> int:
+        return int(self._lib.rts_server_cancel(self.h, ticket))
+
+    def wait(self, ticket, timeout_ms: float = 60000.0):
+        """Blocks until done; returns (submit_ms, start_ms, done_ms)."""
+        st = RequestStats()
+        r = self._lib.rts_server_wait(self.h, ticket, timeout_ms, C.byref(st))
+        self._keep.pop(ticket, None)
+        if r != 0:
+            raise RtsError(r, "server_wait")
+        return st.submit_ms, st.start_ms, st.done_ms

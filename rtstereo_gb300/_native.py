@@ -98,6 +98,13 @@ SIGNATURES = {
     "rts_params_default": (None, [C.POINTER(Params)]),
     "rts_pipeline_run": (i, [p, i, C.POINTER(Pair), C.POINTER(Params), C.POINTER(Out)]),
     "rts_batch_run": (i, [p, i, C.POINTER(Pair), C.POINTER(Params), C.POINTER(Out)]),
+    "rts_server_create": (i, [PP, p, C.POINTER(ServerConfig)]),
+    "rts_server_destroy": (None, [p]),
+    "rts_server_submit": (i, [p, C.POINTER(Pair), C.POINTER(Params), C.POINTER(Out), C.POINTER(u64)]),
+    "rts_server_poll": (i, [p, u64]),
+    "rts_server_wait": (i, [p, u64, d, C.POINTER(RequestStats)]),
+    "rts_server_cancel": (i, [p, u64]),
+    "rts_server_progress": (i, [p]),
     "rts_synth_pair": (i, [u64, i, i, i, i, i, f, i, p, p, p]),
     "rts_gray_to_rgb": (None, [p, p, i, i]),
     "rts_rgb_to_lab": (None, [p, p, i, i]),

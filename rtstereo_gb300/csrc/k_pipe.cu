@@ -8,67 +8,14 @@
 //   k_prep_records  per pixel one 16-byte record: 64-bit census code, packed
 //                   RGB, packed cross arms (l | r<<8 | t<<16 | b<<24)
 //   k_cost_volume   AD / census / AD+census(CombineCost) cost volume from records
-//   k_cross_hseg    cost -> running sum along x (seq/CrossBasedAggregation.cpp:117-125)
-//                   -> row segment P[x+r]-P[x-l-1] (:151-160), one warp per
-//                   (row, 32 disparities), running sums kept in a shared-memory ring
-//   k_cross_vert    vertical sum of row segments / pixel count (:140-167) and the
-//                   first strict arg-min over d (seq/WTA.cpp:15-22), one warp per
-//                   (column, 32 disparities), segments kept in a shared-memory ring
+//   (the cross-based stages work over view tables and live in k_batch.cu)
 //   k_aw_wta        adaptive-weight aggregation (seq/AdaptiveWeightAggregation.cpp:73-111)
 //                   over 64-pixel x 64-disparity tiles, weights made on the fly from
 //                   Lab + host tables, and the arg-min over d
-#include <cuda_fp16.h>
-
-#include "rts_common.cuh"
+#include "rts_fused.cuh"
 #include "rts_pipe.h"
 
 namespace rts {
-
-// ---------------------------------------------------------------------------
-// cost of one (ref pixel, target pixel) pair from records
-
-struct CostCfg {
-    int k1, k2;        // RTS_COST_AD / RTS_COST_CENSUS; k2 may be RTS_COST_NONE
-    int trunc1;        // truncated AD for the first cost (cross-based aggregation)
-    float trunc;
-    const float *lut1, *lut2;
-    float l1, l2;
-    int int_path;      // 1: both costs are integers < kCombineLut (integral truncation)
-    int itrunc;        // integral truncation, or a large value when not truncating
-};
-
-// Integer value of one cost from records: SAD of the packed RGB bytes (the
-// fourth byte is zero) or the census Hamming distance.
-__device__ __forceinline__ int rec_icost(int kind, const uint4 &a, const uint4 &b, int itrunc) {
-    if (kind == RTS_COST_CENSUS) return __popc(a.x ^ b.x) + __popc(a.y ^ b.y);
-    return imin((int)__vsadu4(a.z, b.z), itrunc);
-}
-
-__device__ __forceinline__ float rec_cost(int kind, const uint4 &a, const uint4 &b, int use_trunc, float trunc) {
-    if (kind == RTS_COST_CENSUS) {
-        const uint64_t ca = ((uint64_t)a.y << 32) | a.x, cb = ((uint64_t)b.y << 32) | b.x;
-        return (float)__popcll(ca ^ cb);  // seq/CensusTransform.cpp:52-60
-    }
-    // seq/PixelBasedCost.cpp:86-91 / :106-112 with normOrNot = 0
-    const int sad = abs((int)(a.z & 0xff) - (int)(b.z & 0xff)) + abs((int)((a.z >> 8) & 0xff) - (int)((b.z >> 8) & 0xff)) +
-                    abs((int)((a.z >> 16) & 0xff) - (int)((b.z >> 16) & 0xff));
-    float v = (float)sad;
-    if (use_trunc) v = (v > trunc) ? trunc : v;
-    return v;
-}
-
-__device__ __forceinline__ float pair_cost(const uint4 &a, const uint4 &b, const CostCfg &c) {
-    const float v1 = rec_cost(c.k1, a, b, c.trunc1, c.trunc);
-    if (c.k2 == RTS_COST_NONE) return v1;
-    const float v2 = rec_cost(c.k2, a, b, 0, 0.f);
-    return __fadd_rn(combine_term(v1, c.lut1, c.l1), combine_term(v2, c.lut2, c.l2));  // seq/CombineCost.cpp:23
-}
-
-template <typename T> __device__ __forceinline__ T to_store(float v);
-template <> __device__ __forceinline__ float to_store<float>(float v) { return v; }
-template <> __device__ __forceinline__ __half to_store<__half>(float v) { return __float2half_rn(v); }
-__device__ __forceinline__ float to_f32(float v) { return v; }
-__device__ __forceinline__ float to_f32(__half v) { return __half2float(v); }
 
 // ---------------------------------------------------------------------------
 __global__ void k_prep_records(const uint8_t *__restrict__ gray, const uint8_t *__restrict__ rgb,
@@ -124,212 +71,6 @@ __global__ void k_cost_volume(const uint4 *__restrict__ rr, const uint4 *__restr
     const int xt = tar_col(x, d, W, 1);
     const uint4 a = rr[(size_t)y * W + x], b = rt[(size_t)y * W + xt];
     vol[((size_t)y * W + x) * D + d] = to_store<T>(pair_cost(a, b, cfg));
-}
-
-// ---------------------------------------------------------------------------
-// Cross-based aggregation, horizontal part.  Lane = disparity.  For each x in
-// order: C(x,d), P = P + C (running sum, the reference's in-place prefix,
-// seq/CrossBasedAggregation.cpp:117-125).  The segment of column xs is
-// P[xs+r] - P[xs-l-1] (:151-160) with l, r the min of the ref arm at xs and the
-// target arm at xs-d.  Work goes in 16-column steps: 16 costs and running sums
-// into registers (only the add chain is serial), then they enter a per-lane
-// 64-entry ring in shared memory and the 16 segments whose right ends are now
-// known are emitted.  The ring holds columns x0-48 .. x0+15, enough for
-// arms <= 23.  Records are staged per warp 32 columns at a time (ref x0..x0+31,
-// target x0-dbase-31 .. x0-dbase+31); the next 32 are fetched into registers
-// while the current ones are consumed.
-constexpr int kRing = 64;
-constexpr int kHsegWarps = 2;  // keeps the static shared memory under 48 KB
-constexpr int kHsegStep = 16;
-constexpr int kHsegMaxArm = (kRing - kHsegStep - 1) >> 1;  // 23; also keeps l+r+1 < 64 and t, b < 32
-
-template <typename ST, bool VOL>
-__global__ void __launch_bounds__(kHsegWarps * 32) k_cross_hseg(const uint4 *__restrict__ rr, const uint4 *__restrict__ rt,
-                                                               const float *__restrict__ vol, ST *__restrict__ seg,
-                                                               uint16_t *__restrict__ geo, int H, int W, int D,
-                                                               CostCfg cfg, int L) {
-    __shared__ float pring[kHsegWarps][kRing][32];
-    __shared__ uint16_t lring[kHsegWarps][kRing][32];
-    __shared__ uint4 recA[kHsegWarps][32];
-    __shared__ uint4 recB[kHsegWarps][64];
-    __shared__ float volS[VOL ? kHsegWarps : 1][VOL ? 32 : 1][33];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int nch = (D + 31) >> 5;
-    const int gw = blockIdx.x * kHsegWarps + warp;
-    if (gw >= H * nch) return;  // only warp-level synchronisation in this kernel
-    const int dbase = (gw % nch) * 32;
-    const int y = gw / nch, d = dbase + lane;
-    const bool active = d < D;
-    const int dd = active ? d : D - 1;
-    const int lo = dd - dbase;
-    const size_t row = (size_t)y * W;
-    float (*P)[32] = pring[warp];
-    uint16_t (*LR)[32] = lring[warp];
-    uint4 *RA = recA[warp], *RB = recB[warp];
-
-    auto emit = [&](int xs) {
-        const uint16_t lr = LR[xs & (kRing - 1)][lane];
-        const int l = lr & 0xff, r = lr >> 8;
-        int xl = xs - l - 1;
-        if (xl < 0) xl = 0;  // seq/CrossBasedAggregation.cpp:153-154
-        const int xr = xs + r;
-        const float s = __fsub_rn(P[xr & (kRing - 1)][lane], P[xl & (kRing - 1)][lane]);
-        if (active) seg[(row + xs) * D + d] = to_store<ST>(s);
-    };
-    auto wrapx = [&](int t) {
-        t %= W;
-        return t < 0 ? t + W : t;
-    };
-    uint4 na, nb0, nb1;
-    auto fetch = [&](int x0) {
-        const int t0 = x0 - dbase - 31;
-        na = rr[row + imin(x0 + lane, W - 1)];
-        nb0 = rt[row + wrapx(t0 + lane)];
-        nb1 = rt[row + wrapx(t0 + 32 + lane)];
-    };
-    fetch(0);
-    float acc = 0.f;
-    for (int x0 = 0; x0 < W; x0 += 32) {
-        __syncwarp();
-        RA[lane] = na;
-        RB[lane] = nb0;
-        RB[lane + 32] = nb1;
-        if constexpr (VOL) {
-#pragma unroll 8
-            for (int u = 0; u < 32; u++)
-                if (x0 + u < W) volS[warp][u][lane] = vol[(row + x0 + u) * D + dd];
-        }
-        __syncwarp();
-        if (x0 + 32 < W) fetch(x0 + 32);
-#pragma unroll 1
-        for (int h = 0; h < 32; h += kHsegStep) {
-            const int xb = x0 + h;
-            if (xb >= W) break;
-            const int n = imin(kHsegStep, W - xb);
-            float pv[kHsegStep];
-            uint16_t lv[kHsegStep];
-#pragma unroll
-            for (int u = 0; u < kHsegStep; u++) {
-                if (u < n) {
-                    const uint4 a = RA[h + u];
-                    // target column x - dd sits at index (h + u) + 31 - lo of the staged range
-                    const uint4 b = RB[h + u + 31 - lo];
-                    float c;
-                    if constexpr (VOL) {
-                        c = volS[warp][h + u][lane];
-                    } else if (cfg.int_path) {
-                        const int v1 = rec_icost(cfg.k1, a, b, cfg.itrunc);
-                        if (cfg.k2 == RTS_COST_NONE) c = (float)v1;
-                        else c = __fadd_rn(__ldg(cfg.lut1 + v1), __ldg(cfg.lut2 + rec_icost(cfg.k2, a, b, 0x7fffffff)));
-                    } else {
-                        c = pair_cost(a, b, cfg);
-                    }
-                    acc = (xb + u == 0) ? c : __fadd_rn(c, acc);  // seq/CrossBasedAggregation.cpp:123
-                    pv[u] = acc;
-                    const int l = imin(arm_l(a.w), arm_l(b.w)), r = imin(arm_r(a.w), arm_r(b.w));
-                    lv[u] = (uint16_t)(l | (r << 8));
-                    // geometry of (y, x, d): row pixel count | vertical arms (top, bottom)
-                    if (active)
-                        geo[(row + xb + u) * D + d] =
-                            (uint16_t)((l + r + 1) | (imin(arm_t(a.w), arm_t(b.w)) << 6) | (imin(arm_b(a.w), arm_b(b.w)) << 11));
-                }
-            }
-#pragma unroll
-            for (int u = 0; u < kHsegStep; u++) {
-                if (u < n) {
-                    P[(xb + u) & (kRing - 1)][lane] = pv[u];
-                    LR[(xb + u) & (kRing - 1)][lane] = lv[u];
-                }
-            }
-            // columns whose right end xs + L is now in the ring
-            const int xs_lo = imax(0, xb - L), xs_hi = xb + n - 1 - L;
-#pragma unroll 4
-            for (int xs = xs_lo; xs <= xs_hi; xs++) emit(xs);
-        }
-    }
-    for (int xs = imax(0, W - L); xs < W; xs++) emit(xs);
-}
-
-// ---------------------------------------------------------------------------
-// Cross-based aggregation, vertical part, fused with the arg-min over d.
-// Block = one column x, output rows y0 .. y0+R-1 (R = 64), 8 warps.  Phase 1
-// copies, for rows y0-L .. y0+R+L-1, the row segments and the geometry words
-// (row pixel count | min top arm << 6 | min bottom arm << 11, written by
-// k_cross_hseg) of all disparities into shared memory: 16-byte loads, all in
-// flight together.  Phase 2 gives each warp whole output rows: for every
-// 32-disparity chunk the lanes sum their cross rows top to bottom and divide;
-// the chunk minimum comes from one redux.min over order-preserving keys plus a
-// ballot (lowest lane = lowest d); chunks combine in increasing d, strict <.
-constexpr int kVertThreads = 256;
-constexpr int kVertRows = 64;
-
-__device__ __forceinline__ uint32_t order_key(float v) {
-    const uint32_t u = __float_as_uint(__fadd_rn(v, 0.0f));  // -0 -> +0
-    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
-}
-
-template <typename ST>
-__global__ void __launch_bounds__(kVertThreads) k_cross_vert(const ST *__restrict__ seg, const uint16_t *__restrict__ geo,
-                                                            uint16_t *__restrict__ raw, int *__restrict__ row_last,
-                                                            int H, int W, int D, int L, int R) {
-    extern __shared__ __align__(16) unsigned char vsm[];
-    const int x = blockIdx.y;
-    const int y0 = blockIdx.x * R, y1 = imin(H, y0 + R);
-    const int ya0 = imax(0, y0 - L), ya1 = imin(H, y1 + L);
-    const int nr = ya1 - ya0;
-    ST *S = reinterpret_cast<ST *>(vsm);
-    uint16_t *G = reinterpret_cast<uint16_t *>(vsm + (size_t)(R + 2 * L) * D * sizeof(ST));
-    // phase 1: rows ya0..ya1-1 of column x are D-element runs at stride W*D
-    {
-        constexpr int SV = 16 / sizeof(ST);  // elements per 16-byte vector
-        const int sv_row = D / SV, g_row = D / 8;
-        const int ns = nr * sv_row, ng = nr * g_row;
-        for (int c = threadIdx.x; c < ns + ng; c += kVertThreads) {
-            if (c < ns) {
-                const int ri = c / sv_row, k = c - ri * sv_row;
-                reinterpret_cast<uint4 *>(S + (size_t)ri * D)[k] =
-                    __ldcs(reinterpret_cast<const uint4 *>(seg + ((size_t)(ya0 + ri) * W + x) * D) + k);
-            } else {
-                const int c2 = c - ns;
-                const int ri = c2 / g_row, k = c2 - ri * g_row;
-                reinterpret_cast<uint4 *>(G + (size_t)ri * D)[k] =
-                    __ldcs(reinterpret_cast<const uint4 *>(geo + ((size_t)(ya0 + ri) * W + x) * D) + k);
-            }
-        }
-    }
-    __syncthreads();
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (int yo = y0 + warp; yo < y1; yo += kVertThreads / 32) {
-        const int ro = yo - ya0;
-        uint32_t best_key = 0xffffffffu;
-        int best_d = 0;
-        for (int d0 = 0; d0 < D; d0 += 32) {
-            const int d = d0 + lane;
-            uint32_t key = 0xffffffffu;
-            if (d < D) {
-                const int g = G[ro * D + d];
-                const int t = (g >> 6) & 31, bo = g >> 11;
-                float sum = 0.f;
-                int cnt = 0;
-                for (int r = ro - t; r <= ro + bo; r++) {  // seq/CrossBasedAggregation.cpp:146-164
-                    sum = __fadd_rn(sum, to_f32(S[r * D + d]));
-                    cnt += G[r * D + d] & 63;
-                }
-                key = order_key(__fdiv_rn(sum, (float)cnt));  // :166
-            }
-            const uint32_t m = __reduce_min_sync(0xffffffffu, key);
-            if (m < best_key) {  // strict: an earlier chunk keeps ties
-                const unsigned hit = __ballot_sync(0xffffffffu, key == m);
-                best_key = m;
-                best_d = d0 + __ffs(hit) - 1;
-            }
-        }
-        if (lane == 0) {
-            const bool found = best_d != 0;  // some d >= 1 strictly below cost[0]
-            raw[(size_t)yo * W + x] = found ? (uint16_t)(0x100 | best_d) : (uint16_t)0;
-            if (found) atomicMax(row_last + yo, x);
-        }
-    }
 }
 
 // ---------------------------------------------------------------------------
@@ -562,8 +303,6 @@ __global__ void __launch_bounds__(kAwThreads) k_aw_wta(const CT *__restrict__ vo
 // ---------------------------------------------------------------------------
 // host orchestration
 
-bool cross_fused_supported(const rts_params &p);
-
 static bool fast_kind(int k) { return k == RTS_COST_AD || k == RTS_COST_CENSUS; }
 
 bool fast_costs(const rts_params &p) {
@@ -621,56 +360,10 @@ rts_status cost_volume_fast(rts_ctx *c, const rts_params &p, int H, int W, const
     return check_launch(c, "cost_volume");
 }
 
-template <typename ST>
-static void launch_vert(cudaStream_t s, const ST *seg, const uint16_t *geo, uint16_t *raw, int *rl, int H, int W, int D,
-                        int L) {
-    const int R = kVertRows;
-    const size_t smem = (size_t)(R + 2 * L) * D * (sizeof(ST) + 2);
-    cudaFuncSetAttribute(k_cross_vert<ST>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k_cross_vert<ST><<<dim3((H + R - 1) / R, W), kVertThreads, smem, s>>>(seg, geo, raw, rl, H, W, D, L, R);
-}
-
 bool cross_fused_supported(const rts_params &p) {
-    // 16-byte row copies in the vertical kernel need D a multiple of 8; the ring
-    // of the horizontal kernel bounds the arm length
-    return p.cross_arm <= kHsegMaxArm && p.disp_range % 8 == 0;
-}
-
-rts_status cross_fused(rts_ctx *c, const rts_params &p, int H, int W, const uint4 *rr, const uint4 *rt,
-                       const uint32_t *ar, const uint32_t *at, const float *vol, uint16_t *raw, int *rl) {
-    (void)ar;
-    (void)at;
-    const int D = p.disp_range, L = p.cross_arm;
-    const bool half = p.precision == RTS_PREC_F16;
-    CostCfg cfg;
-    RTS_TRY(cost_cfg(c, p, &cfg));
-    void *seg, *geo;
-    const size_t ne = (size_t)H * W * D;
-    RTS_TRY(scratch(c, SL_V_SEG, ne * (half ? 2 : 4), &seg));
-    RTS_TRY(scratch(c, SL_V_COST2, ne * 2, &geo));
-    const int nch = (D + 31) / 32;
-    const unsigned blocks = (unsigned)((H * nch + kHsegWarps - 1) / kHsegWarps);
-    {
-        StageScope sc(c, "cross_hseg");
-        auto go = [&](auto kern, auto *sp) {
-            kern<<<blocks, kHsegWarps * 32, 0, c->stream>>>(rr, rt, vol, sp, (uint16_t *)geo, H, W, D, cfg, L);
-        };
-        if (half) {
-            if (vol) go(k_cross_hseg<__half, true>, (__half *)seg);
-            else go(k_cross_hseg<__half, false>, (__half *)seg);
-        } else {
-            if (vol) go(k_cross_hseg<float, true>, (float *)seg);
-            else go(k_cross_hseg<float, false>, (float *)seg);
-        }
-        count_launch(c);
-    }
-    {
-        StageScope sc(c, "cross_vert_wta");
-        if (half) launch_vert<__half>(c->stream, (const __half *)seg, (const uint16_t *)geo, raw, rl, H, W, D, L);
-        else launch_vert<float>(c->stream, (const float *)seg, (const uint16_t *)geo, raw, rl, H, W, D, L);
-        count_launch(c);
-    }
-    return check_launch(c, "cross_fused");
+    // 16-byte row copies in the vertical kernel need D a multiple of 8; the
+    // 64-entry ring of the horizontal kernel bounds the arm length (k_batch.cu)
+    return p.cross_arm <= 23 && p.disp_range % 8 == 0;
 }
 
 rts_status aw_fused(rts_ctx *c, const rts_params &p, int H, int W, const void *vol, int half, const uint8_t *labr,

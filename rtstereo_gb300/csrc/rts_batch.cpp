@@ -1,20 +1,683 @@
-// rts_batch.cpp -- batched form and serving loop (first version: pairs run
-// one after another on the context stream).
+// rts_batch.cpp -- batched form (rts_batch_run) and the serving loop
+// (rts_server_*) of the cross-based pipeline.
+//
+// Batched form: the n pairs become 2n views of one view table; every stage is
+// one persistent launch over all views (k_batch.cu).  The five launches (and
+// the reset of the row summaries) are captured once per batch shape into a
+// CUDA graph; a later call with the same shape re-uploads only the view table
+// (its image and output pointers) and replays the graph.  The tile parameters
+// of the stages (rows per vertical block, persistent blocks per SM) are picked
+// per batch shape by timing the candidates on the first call (autotuner).
+//
+// Serving loop: requests are admitted in arrival order while a slot and enough
+// of the server's device pool (cost-volume bytes of the request, e.g. a 40 GB
+// budget) are free; admitted requests are launched as batches on a ring of
+// streams, so a batch formed from requests that arrived while others were
+// running overlaps with them on the device.  Completion is polled with events.
+#include <string.h>
+
+#include <chrono>
+#include <deque>
+#include <map>
+#include <memory>
+#include <string>
+#include <unordered_map>
+
 #include "rts_internal.h"
+#include "rts_pipe.h"
+#include "rts_views.h"
+
+namespace rts {
+rts_status validate_params(rts_ctx *c, const rts_params &p, int H, int W);
+}
 
 using namespace rts;
 
+namespace {
+
+bool same_except_d(const rts_params &a, const rts_params &b) {
+    rts_params x = a, y = b;
+    x.disp_range = y.disp_range = 0;
+    return memcmp(&x, &y, sizeof(rts_params)) == 0;
+}
+
+std::string shape_key(int n, const rts_pair *pairs, const rts_params *params) {
+    std::string k;
+    k.reserve(16 * n + sizeof(rts_params));
+    k.append((const char *)&params[0], sizeof(rts_params));
+    for (int i = 0; i < n; i++) {
+        const int d[4] = {pairs[i].width, pairs[i].height, params[i].disp_range,
+                          pairs[i].left_rgb ? 1 : 0};
+        k.append((const char *)d, sizeof(d));
+    }
+    return k;
+}
+
+struct GraphEntry {
+    cudaGraphExec_t exec = nullptr;
+    void *arena = nullptr;     // the arena the graph's kernels and memset address
+    size_t arena_bytes = 0;
+    CrossTune tune;
+    uint64_t launches = 0;     // kernel launches inside the graph
+};
+
+struct GraphCache {
+    std::unordered_map<std::string, GraphEntry> graphs;
+    std::unordered_map<std::string, CrossTune> tunes;
+    ~GraphCache() {
+        for (auto &kv : graphs)
+            if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
+    }
+};
+
+GraphCache *cache_of(rts_ctx *c) {
+    if (!c->graph_cache) c->graph_cache = new GraphCache();
+    return (GraphCache *)c->graph_cache;
+}
+
+// Fills image/output pointers of the 2n views of n pairs.
+void fill_views(ViewBatch &b, int n, const rts_pair *pairs, const rts_out *outs, int right) {
+    for (int i = 0; i < n; i++) {
+        const rts_pair &q = pairs[i];
+        ViewDesc &l = b.views[right ? 2 * i : i];
+        l.gref = q.left_gray; l.gtar = q.right_gray; l.cref = q.left_rgb; l.ctar = q.right_rgb;
+        if (!q.left_rgb || !q.right_rgb) l.cref = l.ctar = nullptr;
+        l.mirror = 0;
+        l.disp = outs[i].disp_left;
+        l.vol = nullptr;
+        if (right) {
+            ViewDesc &r = b.views[2 * i + 1];
+            r.gref = q.right_gray; r.gtar = q.left_gray; r.cref = l.ctar; r.ctar = l.cref;
+            r.mirror = 1;
+            r.disp = outs[i].disp_right;
+            r.vol = nullptr;
+            l.mask = outs[i].mask;
+            l.partner = 2 * i + 1;
+        }
+    }
+}
+
+void view_dims(int n, const rts_pair *pairs, const rts_params *params, int right, std::vector<int> &W,
+               std::vector<int> &H, std::vector<int> &D) {
+    const int nv = right ? 2 * n : n;
+    W.resize(nv);
+    H.resize(nv);
+    D.resize(nv);
+    for (int i = 0; i < n; i++)
+        for (int k = 0; k < (right ? 2 : 1); k++) {
+            const int v = right ? 2 * i + k : i;
+            W[v] = pairs[i].width;
+            H[v] = pairs[i].height;
+            D[v] = params[i].disp_range;
+        }
+}
+
+// Candidate tiles of the autotuner.
+const CrossTune kTuneCandidates[] = {{32, 2}, {64, 2}, {128, 2}, {32, 4}, {64, 4}, {128, 4}, {64, 8}};
+
+}  // namespace
+
 extern "C" {
 
-void rts_graph_cache_free(rts_ctx *c) { (void)c; }
+void rts_graph_cache_free(rts_ctx *c) {
+    if (c && c->graph_cache) {
+        delete (GraphCache *)c->graph_cache;
+        c->graph_cache = nullptr;
+    }
+}
 
 rts_status rts_batch_run(rts_ctx *ctx, int n, const rts_pair *pairs, const rts_params *params, rts_out *outs) {
     if (!ctx || n < 0 || (n > 0 && (!pairs || !params || !outs))) return RTS_ERR_INVALID_ARG;
-    for (int i = 0; i < n; i++) {
-        rts_status s = rts_pipeline_run(ctx, RTS_DEVICE, &pairs[i], &params[i], &outs[i]);
-        if (s != RTS_OK) return s;
+    if (n == 0) return RTS_OK;
+    std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+    rts_ctx *c = ctx;
+    if (cudaSetDevice(c->device) != cudaSuccess) return set_error(c, RTS_ERR_CUDA, "cudaSetDevice failed");
+    bool batched = params[0].aggr == RTS_AGGR_CROSS && cross_fused_supported(params[0]) && fast_costs(params[0]);
+    for (int i = 0; i < n && batched; i++) {
+        RTS_TRY(validate_params(c, params[i], pairs[i].height, pairs[i].width));
+        batched = same_except_d(params[0], params[i]) && cross_fused_supported(params[i]) &&
+                  (pairs[i].left_rgb != nullptr) == (pairs[0].left_rgb != nullptr);
+    }
+    if (!batched) {
+        // other configurations: one pipeline run per pair, on the same stream
+        for (int i = 0; i < n; i++) RTS_TRY(rts_pipeline_run(c, RTS_DEVICE, &pairs[i], &params[i], &outs[i]));
+        return RTS_OK;
+    }
+    return batch_views_run(c, n, pairs, params, outs);
+}
+
+}  // extern "C"
+
+// The batched cross-based pipeline on DEVICE buffers: one view table, autotuned
+// tiles, one captured graph per batch shape.  Callers have validated the pairs.
+rts_status rts::batch_views_run(rts_ctx *c, int n, const rts_pair *pairs, const rts_params *params, rts_out *outs) {
+    for (int i = 0; i < n; i++)
+        if (!pairs[i].left_gray || !pairs[i].right_gray || !outs[i].disp_left ||
+            (params[0].right_view && (!outs[i].disp_right || !outs[i].mask)))
+            return set_error(c, RTS_ERR_INVALID_ARG, "null image or output in the batch");
+    const rts_params &p = params[0];
+    const int right = p.right_view ? 1 : 0, half = p.precision == RTS_PREC_F16 ? 1 : 0;
+    const int nv = right ? 2 * n : n;
+    std::vector<int> W, H, D;
+    view_dims(n, pairs, params, right, W, H, D);
+    GraphCache *gc = cache_of(c);
+    const std::string key = shape_key(n, pairs, params);
+    const size_t bytes = views_bytes(W.data(), H.data(), D.data(), nv, half);
+    void *arena;
+    RTS_TRY(scratch(c, SL_BATCH0, bytes, &arena));
+    // the tables the kernels read must hold this lambda pair before any replay
+    const float *l1, *l2;
+    if (p.cost2 != RTS_COST_NONE) RTS_TRY(combine_luts(c, p.lambda1, p.lambda2, &l1, &l2));
+    ViewBatch b;
+    plan_views_at(arena, W.data(), H.data(), D.data(), nv, half, &b);
+    fill_views(b, n, pairs, outs, right);
+    // autotune once per shape: time every candidate on this batch
+    auto tit = gc->tunes.find(key);
+    if (tit == gc->tunes.end()) {
+        const bool timing = c->timing;
+        c->timing = false;
+        CrossTune best = kTuneCandidates[0];
+        float best_ms = 1e30f;
+        cudaEvent_t e0, e1;
+        RTS_CU(c, cudaEventCreate(&e0));
+        RTS_CU(c, cudaEventCreate(&e1));
+        for (const CrossTune &cand : kTuneCandidates) {
+            ViewTable t;
+            RTS_TRY(upload_views(c, b, cand, nullptr, &t));
+            RTS_CU(c, cudaEventRecord(e0, c->stream));
+            RTS_TRY(launch_cross_views(c, p, t, half, 0, b.max_d, cand, b.row_last_all, b.row_last_count));
+            RTS_CU(c, cudaEventRecord(e1, c->stream));
+            RTS_CU(c, cudaEventSynchronize(e1));
+            float ms = 0;
+            RTS_CU(c, cudaEventElapsedTime(&ms, e0, e1));
+            if (ms < best_ms) {
+                best_ms = ms;
+                best = cand;
+            }
+        }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        c->timing = timing;
+        tit = gc->tunes.emplace(key, best).first;
+    }
+    const CrossTune tune = tit->second;
+    ViewTable t;
+    // a pageable upload: the host table may be reused as soon as the copy call returns
+    RTS_TRY(upload_views(c, b, tune, nullptr, &t));
+    if (c->timing) {
+        // stage timing wants an event pair around every kernel: launch directly
+        return launch_cross_views(c, p, t, half, 0, b.max_d, tune, b.row_last_all, b.row_last_count);
+    }
+    GraphEntry &g = gc->graphs[key];
+    if (g.exec && (g.arena != arena || g.arena_bytes != bytes)) {
+        cudaGraphExecDestroy(g.exec);
+        g.exec = nullptr;
+    }
+    if (!g.exec) {
+        // capture the stage launches; the view table is read from device memory,
+        // so later calls only re-upload it before the replay
+        const bool timing = c->timing;
+        c->timing = false;
+        const uint64_t l0 = c->launches.load();
+        cudaGraph_t graph;
+        RTS_CU(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+        rts_status st = launch_cross_views(c, p, t, half, 0, b.max_d, tune, b.row_last_all, b.row_last_count);
+        cudaError_t ce = cudaStreamEndCapture(c->stream, &graph);
+        c->timing = timing;
+        if (st != RTS_OK) return st;
+        RTS_CU(c, ce);
+        ce = cudaGraphInstantiate(&g.exec, graph, 0);
+        cudaGraphDestroy(graph);
+        RTS_CU(c, ce);
+        g.arena = arena;
+        g.arena_bytes = bytes;
+        g.tune = tune;
+        g.launches = c->launches.load() - l0;
+        c->launches.fetch_sub(g.launches);  // counted on every replay instead
+    }
+    {
+        StageScope sc(c, "batch_graph");
+        RTS_CU(c, cudaGraphLaunch(g.exec, c->stream));
+        count_launch(c, (int)g.launches);
     }
     return RTS_OK;
+}
+
+// ===========================================================================
+// serving loop
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+// first-fit allocator over one device pool (the server's HBM budget)
+struct Pool {
+    unsigned char *base = nullptr;
+    size_t size = 0;
+    std::map<size_t, size_t> free_;  // offset -> length
+    size_t used = 0;
+    bool init(size_t bytes) {
+        if (cudaMalloc(&base, bytes) != cudaSuccess) {
+            cudaGetLastError();
+            base = nullptr;
+            return false;
+        }
+        size = bytes;
+        free_[0] = bytes;
+        return true;
+    }
+    void *alloc(size_t bytes) {
+        bytes = (bytes + 255) & ~size_t(255);
+        for (auto it = free_.begin(); it != free_.end(); ++it) {
+            if (it->second >= bytes) {
+                const size_t off = it->first, len = it->second;
+                free_.erase(it);
+                if (len > bytes) free_[off + bytes] = len - bytes;
+                used += bytes;
+                return base + off;
+            }
+        }
+        return nullptr;
+    }
+    void release(void *p, size_t bytes) {
+        if (!p) return;
+        bytes = (bytes + 255) & ~size_t(255);
+        size_t off = (unsigned char *)p - base;
+        used -= bytes;
+        auto it = free_.emplace(off, bytes).first;
+        auto nx = std::next(it);
+        if (nx != free_.end() && it->first + it->second == nx->first) {
+            it->second += nx->second;
+            free_.erase(nx);
+        }
+        if (it != free_.begin()) {
+            auto pv = std::prev(it);
+            if (pv->first + pv->second == it->first) {
+                pv->second += it->second;
+                free_.erase(it);
+            }
+        }
+    }
+    ~Pool() {
+        if (base) cudaFree(base);
+    }
+};
+
+enum ReqState { RQ_PENDING, RQ_RUNNING, RQ_DONE, RQ_CANCELLED, RQ_FAILED };
+
+struct Request {
+    uint64_t ticket;
+    rts_pair pair;
+    rts_params params;
+    rts_out out;               // caller's host buffers
+    unsigned char *h_in = nullptr;  // pinned copy of the inputs: gray L, gray R, (rgb L, rgb R)
+    unsigned char *h_out = nullptr; // pinned outputs: disp L, disp R, mask
+    size_t in_bytes = 0, out_bytes = 0;
+    void *d_mem = nullptr;     // device: inputs + outputs
+    size_t d_bytes = 0;
+    int state = RQ_PENDING;
+    int batch = -1;
+    double t_submit = 0, t_start = 0, t_done = 0;
+};
+
+struct Batch {
+    std::vector<uint64_t> tickets;
+    void *arena = nullptr;
+    size_t arena_bytes = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t done = nullptr;
+    bool active = false;
+};
+
+}  // namespace
+
+struct rts_server {
+    rts_ctx *ctx = nullptr;
+    rts_server_config cfg{};
+    Pool pool;
+    std::vector<cudaStream_t> streams;
+    std::vector<Batch> batches;
+    std::unordered_map<uint64_t, std::unique_ptr<Request>> reqs;
+    std::deque<uint64_t> queue;
+    uint64_t next_ticket = 1;
+    int inflight = 0;
+    int next_stream = 0;
+    rts_params base_params{};
+    bool have_params = false;
+    Clock::time_point t0 = Clock::now();
+    std::mutex mu;
+    double now_ms() const { return std::chrono::duration<double, std::milli>(Clock::now() - t0).count(); }
+};
+
+namespace {
+
+size_t request_device_bytes(const Request &r) {
+    const size_t np = (size_t)r.pair.width * r.pair.height;
+    return ((r.in_bytes + 255) & ~size_t(255)) + ((3 * np + 255) & ~size_t(255));
+}
+
+void finish_batch(rts_server *s, Batch &bt) {
+    for (uint64_t tk : bt.tickets) {
+        auto it = s->reqs.find(tk);
+        if (it == s->reqs.end()) continue;
+        Request &r = *it->second;
+        const size_t np = (size_t)r.pair.width * r.pair.height;
+        if (r.state == RQ_RUNNING) {
+            memcpy(r.out.disp_left, r.h_out, np);
+            if (r.params.right_view) {
+                memcpy(r.out.disp_right, r.h_out + np, np);
+                memcpy(r.out.mask, r.h_out + 2 * np, np);
+            }
+            r.state = RQ_DONE;
+        }
+        r.t_done = s->now_ms();
+        s->pool.release(r.d_mem, r.d_bytes);
+        r.d_mem = nullptr;
+        s->inflight--;
+    }
+    s->pool.release(bt.arena, bt.arena_bytes);
+    bt.arena = nullptr;
+    bt.tickets.clear();
+    bt.active = false;
+}
+
+// Launches the requests in `ids` as one batch on the next free stream.
+rts_status launch_batch(rts_server *s, std::vector<Request *> &ids) {
+    rts_ctx *c = s->ctx;
+    int slot = -1;
+    for (int k = 0; k < (int)s->batches.size(); k++) {
+        const int j = (s->next_stream + k) % (int)s->batches.size();
+        if (!s->batches[j].active) {
+            slot = j;
+            break;
+        }
+    }
+    if (slot < 0) return RTS_ERR_BUSY;
+    Batch &bt = s->batches[slot];
+    const int n = (int)ids.size();
+    const rts_params &p = s->base_params;
+    const int right = p.right_view ? 1 : 0, half = p.precision == RTS_PREC_F16 ? 1 : 0;
+    std::vector<rts_pair> pairs(n);
+    std::vector<rts_params> params(n);
+    std::vector<rts_out> outs(n);
+    for (int i = 0; i < n; i++) {
+        Request &r = *ids[i];
+        const size_t np = (size_t)r.pair.width * r.pair.height;
+        unsigned char *d = (unsigned char *)r.d_mem;
+        unsigned char *dout = d + ((r.in_bytes + 255) & ~size_t(255));
+        pairs[i] = r.pair;
+        pairs[i].left_gray = d;
+        pairs[i].right_gray = d + np;
+        pairs[i].left_rgb = r.pair.left_rgb ? d + 2 * np : nullptr;
+        pairs[i].right_rgb = r.pair.right_rgb ? d + 5 * np : nullptr;
+        pairs[i].left_lab = pairs[i].right_lab = nullptr;
+        params[i] = r.params;
+        outs[i] = rts_out{dout, dout + np, dout + 2 * np, nullptr};
+    }
+    std::vector<int> W, H, D;
+    view_dims(n, pairs.data(), params.data(), right, W, H, D);
+    const int nv = right ? 2 * n : n;
+    bt.arena_bytes = views_bytes(W.data(), H.data(), D.data(), nv, half);
+    bt.arena = s->pool.alloc(bt.arena_bytes);
+    if (!bt.arena) return RTS_ERR_BUSY;
+    cudaStream_t saved = c->stream;
+    c->stream = s->streams[slot];
+    rts_status st = RTS_OK;
+    for (int i = 0; i < n && st == RTS_OK; i++) {
+        Request &r = *ids[i];
+        if (cudaMemcpyAsync(r.d_mem, r.h_in, r.in_bytes, cudaMemcpyHostToDevice, c->stream) != cudaSuccess)
+            st = set_error(c, RTS_ERR_CUDA, "server H2D copy failed");
+    }
+    ViewBatch b;
+    if (st == RTS_OK) {
+        plan_views_at(bt.arena, W.data(), H.data(), D.data(), nv, half, &b);
+        fill_views(b, n, pairs.data(), outs.data(), right);
+        ViewTable t;
+        CrossTune tune;
+        st = upload_views(c, b, tune, nullptr, &t);
+        if (st == RTS_OK) st = launch_cross_views(c, p, t, half, 0, b.max_d, tune, b.row_last_all, b.row_last_count);
+    }
+    for (int i = 0; i < n && st == RTS_OK; i++) {
+        Request &r = *ids[i];
+        if (cudaMemcpyAsync(r.h_out, outs[i].disp_left, r.out_bytes, cudaMemcpyDeviceToHost, c->stream) != cudaSuccess)
+            st = set_error(c, RTS_ERR_CUDA, "server D2H copy failed");
+    }
+    if (st == RTS_OK && cudaEventRecord(bt.done, c->stream) != cudaSuccess) st = RTS_ERR_CUDA;
+    c->stream = saved;
+    if (st != RTS_OK) {
+        s->pool.release(bt.arena, bt.arena_bytes);
+        bt.arena = nullptr;
+        return st;
+    }
+    const double t = s->now_ms();
+    for (Request *r : ids) {
+        r->state = RQ_RUNNING;
+        r->batch = slot;
+        r->t_start = t;
+        bt.tickets.push_back(r->ticket);
+    }
+    bt.active = true;
+    bt.stream = s->streams[slot];
+    s->next_stream = (slot + 1) % (int)s->batches.size();
+    return RTS_OK;
+}
+
+rts_status progress_locked(rts_server *s) {
+    // completions
+    for (Batch &bt : s->batches) {
+        if (!bt.active) continue;
+        const cudaError_t q = cudaEventQuery(bt.done);
+        if (q == cudaSuccess) finish_batch(s, bt);
+        else if (q != cudaErrorNotReady) return cuda_check(s->ctx, q, "server batch");
+    }
+    // admission in arrival order while a stream, a slot and device memory are free
+    bool free_stream = false;
+    for (Batch &bt : s->batches) free_stream |= !bt.active;
+    if (!free_stream) return RTS_OK;
+    std::vector<Request *> batch;
+    size_t batch_bytes = 0;
+    while (!s->queue.empty() && (int)batch.size() < s->cfg.max_batch && s->inflight < s->cfg.max_inflight) {
+        Request &r = *s->reqs[s->queue.front()];
+        if (r.state == RQ_CANCELLED) {
+            s->queue.pop_front();
+            continue;
+        }
+        // the request's own buffers plus its share of the batch scratch
+        int Wv[2] = {r.pair.width, r.pair.width}, Hv[2] = {r.pair.height, r.pair.height},
+            Dv[2] = {r.params.disp_range, r.params.disp_range};
+        const size_t need_scratch = views_bytes(Wv, Hv, Dv, r.params.right_view ? 2 : 1,
+                                                s->base_params.precision == RTS_PREC_F16);
+        const size_t need = request_device_bytes(r);
+        if (s->pool.used + batch_bytes + need + need_scratch + 65536 > s->pool.size) break;  // wait for memory
+        r.d_bytes = need;
+        r.d_mem = s->pool.alloc(need);
+        if (!r.d_mem) break;
+        batch_bytes += need_scratch;
+        s->queue.pop_front();
+        s->inflight++;
+        batch.push_back(&r);
+    }
+    if (batch.empty()) return RTS_OK;
+    rts_status st = launch_batch(s, batch);
+    if (st != RTS_OK) {
+        // put the requests back at the head of the queue
+        for (auto it = batch.rbegin(); it != batch.rend(); ++it) {
+            s->pool.release((*it)->d_mem, (*it)->d_bytes);
+            (*it)->d_mem = nullptr;
+            s->inflight--;
+            s->queue.push_front((*it)->ticket);
+        }
+        return st == RTS_ERR_BUSY ? RTS_OK : st;
+    }
+    return RTS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+rts_status rts_server_create(rts_server **out, rts_ctx *ctx, const rts_server_config *cfg) {
+    if (!out || !ctx || !cfg || cfg->hbm_budget == 0 || cfg->max_inflight <= 0 || cfg->max_batch <= 0)
+        return RTS_ERR_INVALID_ARG;
+    *out = nullptr;
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return RTS_ERR_CUDA;
+    auto *s = new rts_server();
+    s->ctx = ctx;
+    s->cfg = *cfg;
+    if (!s->pool.init(cfg->hbm_budget)) {
+        delete s;
+        return set_error(ctx, RTS_ERR_OOM, "cannot reserve the server's device pool");
+    }
+    const int nstreams = 3;
+    s->streams.resize(nstreams);
+    s->batches.resize(nstreams);
+    for (int i = 0; i < nstreams; i++) {
+        if (cudaStreamCreateWithFlags(&s->streams[i], cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&s->batches[i].done, cudaEventDisableTiming) != cudaSuccess) {
+            rts_server_destroy(s);
+            return RTS_ERR_CUDA;
+        }
+    }
+    *out = s;
+    return RTS_OK;
+}
+
+void rts_server_destroy(rts_server *s) {
+    if (!s) return;
+    cudaSetDevice(s->ctx->device);
+    for (auto st : s->streams)
+        if (st) cudaStreamSynchronize(st);
+    for (auto &kv : s->reqs) {
+        if (kv.second->h_in) cudaFreeHost(kv.second->h_in);
+        if (kv.second->h_out) cudaFreeHost(kv.second->h_out);
+    }
+    for (auto &b : s->batches)
+        if (b.done) cudaEventDestroy(b.done);
+    for (auto st : s->streams)
+        if (st) cudaStreamDestroy(st);
+    delete s;
+}
+
+rts_status rts_server_submit(rts_server *s, const rts_pair *pair, const rts_params *params, rts_out *out,
+                             uint64_t *ticket) {
+    if (!s || !pair || !params || !out || !ticket) return RTS_ERR_INVALID_ARG;
+    std::lock_guard<std::mutex> g(s->mu);
+    std::lock_guard<std::recursive_mutex> lk(s->ctx->mu);
+    rts_ctx *c = s->ctx;
+    RTS_TRY(validate_params(c, *params, pair->height, pair->width));
+    if (params->aggr != RTS_AGGR_CROSS || !cross_fused_supported(*params) || !fast_costs(*params))
+        return set_error(c, RTS_ERR_INVALID_ARG, "the serving loop runs the fused cross-based pipeline");
+    if (!s->have_params) {
+        s->base_params = *params;
+        s->have_params = true;
+    } else if (!same_except_d(s->base_params, *params)) {
+        return set_error(c, RTS_ERR_INVALID_ARG, "requests of one server share all parameters but disp_range");
+    }
+    if (!pair->left_gray || !pair->right_gray || !out->disp_left || (params->right_view && (!out->disp_right || !out->mask)))
+        return set_error(c, RTS_ERR_INVALID_ARG, "null image or output");
+    auto r = std::make_unique<Request>();
+    r->ticket = s->next_ticket++;
+    r->pair = *pair;
+    r->params = *params;
+    r->out = *out;
+    const size_t np = (size_t)pair->width * pair->height;
+    const bool rgb = pair->left_rgb && pair->right_rgb;
+    r->pair.left_rgb = rgb ? pair->left_rgb : nullptr;
+    r->pair.right_rgb = rgb ? pair->right_rgb : nullptr;
+    r->in_bytes = np * (rgb ? 8 : 2);
+    r->out_bytes = np * 3;
+    // admission control also covers requests that could never fit
+    int Wv[2] = {pair->width, pair->width}, Hv[2] = {pair->height, pair->height},
+        Dv[2] = {params->disp_range, params->disp_range};
+    if (request_device_bytes(*r) + views_bytes(Wv, Hv, Dv, params->right_view ? 2 : 1,
+                                               params->precision == RTS_PREC_F16) > s->pool.size)
+        return set_error(c, RTS_ERR_BUSY, "request larger than the server's HBM budget");
+    if (cudaHostAlloc((void **)&r->h_in, r->in_bytes, cudaHostAllocDefault) != cudaSuccess ||
+        cudaHostAlloc((void **)&r->h_out, r->out_bytes, cudaHostAllocDefault) != cudaSuccess) {
+        if (r->h_in) cudaFreeHost(r->h_in);
+        return set_error(c, RTS_ERR_OOM, "pinned host memory");
+    }
+    memcpy(r->h_in, pair->left_gray, np);
+    memcpy(r->h_in + np, pair->right_gray, np);
+    if (rgb) {
+        memcpy(r->h_in + 2 * np, pair->left_rgb, 3 * np);
+        memcpy(r->h_in + 5 * np, pair->right_rgb, 3 * np);
+    }
+    r->t_submit = s->now_ms();
+    *ticket = r->ticket;
+    s->queue.push_back(r->ticket);
+    s->reqs.emplace(r->ticket, std::move(r));
+    return progress_locked(s);
+}
+
+rts_status rts_server_progress(rts_server *s) {
+    if (!s) return RTS_ERR_INVALID_ARG;
+    std::lock_guard<std::mutex> g(s->mu);
+    std::lock_guard<std::recursive_mutex> lk(s->ctx->mu);
+    if (cudaSetDevice(s->ctx->device) != cudaSuccess) return RTS_ERR_CUDA;
+    return progress_locked(s);
+}
+
+int rts_server_poll(rts_server *s, uint64_t ticket) {
+    if (!s) return -(int)RTS_ERR_INVALID_ARG;
+    rts_status st = rts_server_progress(s);
+    if (st != RTS_OK) return -(int)st;
+    std::lock_guard<std::mutex> g(s->mu);
+    auto it = s->reqs.find(ticket);
+    if (it == s->reqs.end()) return -(int)RTS_ERR_INVALID_ARG;
+    switch (it->second->state) {
+    case RQ_DONE: return 1;
+    case RQ_CANCELLED: return -(int)RTS_ERR_CANCELLED;
+    case RQ_FAILED: return -(int)RTS_ERR_CUDA;
+    }
+    return 0;
+}
+
+rts_status rts_server_wait(rts_server *s, uint64_t ticket, double timeout_ms, rts_request_stats *stats) {
+    if (!s) return RTS_ERR_INVALID_ARG;
+    const double t_end = s->now_ms() + timeout_ms;
+    for (;;) {
+        const int r = rts_server_poll(s, ticket);
+        if (r == -(int)RTS_ERR_CANCELLED) {
+            std::lock_guard<std::mutex> g(s->mu);
+            auto it = s->reqs.find(ticket);
+            if (it != s->reqs.end() && it->second->d_mem == nullptr) {  // no longer on the device
+                cudaFreeHost(it->second->h_in);
+                cudaFreeHost(it->second->h_out);
+                s->reqs.erase(it);
+            }
+            return RTS_ERR_CANCELLED;
+        }
+        if (r < 0) return (rts_status)(-r);
+        if (r == 1) break;
+        if (s->now_ms() > t_end) return RTS_ERR_TIMEOUT;
+    }
+    std::lock_guard<std::mutex> g(s->mu);
+    auto it = s->reqs.find(ticket);
+    Request &r = *it->second;
+    if (stats) *stats = rts_request_stats{r.t_submit, r.t_start, r.t_done};
+    // the result has been delivered: the request's host staging can go
+    cudaFreeHost(r.h_in);
+    cudaFreeHost(r.h_out);
+    s->reqs.erase(it);
+    return RTS_OK;
+}
+
+rts_status rts_server_cancel(rts_server *s, uint64_t ticket) {
+    if (!s) return RTS_ERR_INVALID_ARG;
+    std::lock_guard<std::mutex> g(s->mu);
+    auto it = s->reqs.find(ticket);
+    if (it == s->reqs.end()) return RTS_ERR_INVALID_ARG;
+    Request &r = *it->second;
+    if (r.state == RQ_PENDING) {
+        r.state = RQ_CANCELLED;  // skipped at admission
+        return RTS_OK;
+    }
+    if (r.state == RQ_RUNNING) {
+        r.state = RQ_CANCELLED;  // the batch finishes on the device; the result is not delivered
+        return RTS_OK;
+    }
+    return RTS_ERR_INVALID_ARG;
 }
 
 }  // extern "C"

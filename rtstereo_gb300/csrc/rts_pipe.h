@@ -8,7 +8,7 @@ namespace rts {
 
 // AD / census (<= 64-bit window) single or combined costs, computed on the fly
 bool fast_costs(const rts_params &p);
-// cross-based (arm <= 23) and adaptive-weight (radius <= 16) aggregation
+// adaptive-weight aggregation (radius <= 16) has a fused per-view path
 bool fused_supported(const rts_params &p, int H, int W);
 
 // 16-byte per-pixel records: census code, packed RGB, packed cross arms
@@ -17,9 +17,8 @@ rts_status prep_records(rts_ctx *c, const rts_params &p, int H, int W, const uin
 // cost volume [H][W][D] (float, or __half when half != 0) from records
 rts_status cost_volume_fast(rts_ctx *c, const rts_params &p, int H, int W, const uint4 *rr, const uint4 *rt,
                             void *vol, int half);
-// cross-based aggregation + arg-min; vol == nullptr computes the cost on the fly
-rts_status cross_fused(rts_ctx *c, const rts_params &p, int H, int W, const uint4 *rr, const uint4 *rt,
-                       const uint32_t *ar, const uint32_t *at, const float *vol, uint16_t *raw, int *row_last);
+// the cross-based pipeline runs over view tables (rts_views.h) when this holds
+bool cross_fused_supported(const rts_params &p);
 // adaptive-weight aggregation + arg-min over a float (half == 0) or __half volume
 rts_status aw_fused(rts_ctx *c, const rts_params &p, int H, int W, const void *vol, int half, const uint8_t *labr,
                     const uint8_t *labt, uint16_t *raw, int *row_last, float *cost_out);

@@ -15,6 +15,7 @@
 
 #include "rts_internal.h"
 #include "rts_pipe.h"
+#include "rts_views.h"
 
 using namespace rts;
 
@@ -120,6 +121,22 @@ static rts_status one_cost(rts_ctx *c, const rts_params &p, int which, bool trun
     return set_error(c, RTS_ERR_INVALID_ARG, "unknown cost");
 }
 
+// cost1 (and cost2 combined, seq/Main.cpp:180-234) into `out` with the module kernels
+static rts_status cost_volume_composed(rts_ctx *c, const rts_params &p, int H, int W, const ViewIn &v, float *out) {
+    const size_t ne = (size_t)H * W * p.disp_range;
+    RTS_TRY(one_cost(c, p, p.cost1, p.aggr == RTS_AGGR_CROSS, H, W, v, out, SL_V_AUX));
+    if (p.cost2 != RTS_COST_NONE) {
+        void *c2v;
+        RTS_TRY(scratch(c, SL_V_COST2, ne * 4, &c2v));
+        RTS_TRY(one_cost(c, p, p.cost2, false, H, W, v, (float *)c2v, SL_TMP2));
+        const float *l1, *l2;
+        RTS_TRY(combine_luts(c, p.lambda1, p.lambda2, &l1, &l2));
+        launch_combine(c->stream, out, (const float *)c2v, (long)ne, l1, l2, p.lambda1, p.lambda2);
+        count_launch(c);
+    }
+    return RTS_OK;
+}
+
 // Composed path for one view: module kernels in the reference's order.
 static rts_status view_composed(rts_ctx *c, const rts_params &p, int H, int W, const ViewIn &v, uint8_t *disp,
                                 int mirror, float *cost_out) {
@@ -200,22 +217,20 @@ static rts_status view_fused(rts_ctx *c, const rts_params &p, int H, int W, cons
     cudaStream_t s = c->stream;
     const bool half = p.precision == RTS_PREC_F16;
     void *recv, *raw, *rl;
-    RTS_TRY(scratch(c, SL_V_REC, np * 40, &recv));
+    RTS_TRY(scratch(c, SL_V_REC, np * 32, &recv));
     uint4 *rr = (uint4 *)recv, *rt = rr + np;
-    uint32_t *ar = (uint32_t *)(rt + np), *at = ar + np;  // compact arms
     RTS_TRY(scratch(c, SL_V_RAW, np * 2, &raw));
     RTS_TRY(scratch(c, SL_V_ROWLAST, (size_t)H * 4, &rl));
     RTS_CU(c, cudaMemsetAsync(rl, 0xff, (size_t)H * 4, s));
     {
         StageScope sc(c, "prep");
-        const bool cross = p.aggr == RTS_AGGR_CROSS;
-        RTS_TRY(prep_records(c, p, H, W, v.gref, v.cref, rr, cross ? ar : nullptr));
-        RTS_TRY(prep_records(c, p, H, W, v.gtar, v.ctar, rt, cross ? at : nullptr));
+        RTS_TRY(prep_records(c, p, H, W, v.gref, v.cref, rr, nullptr));
+        RTS_TRY(prep_records(c, p, H, W, v.gtar, v.ctar, rt, nullptr));
     }
     const bool fast = fast_costs(p);
     const void *vol = nullptr;
     int vol_half = 0;
-    if (!fast || p.aggr == RTS_AGGR_AW) {
+    {
         StageScope sc(c, "cost");
         void *c1v;
         if (fast) {
@@ -224,24 +239,11 @@ static rts_status view_fused(rts_ctx *c, const rts_params &p, int H, int W, cons
             RTS_TRY(cost_volume_fast(c, p, H, W, rr, rt, c1v, vol_half));
         } else {
             RTS_TRY(scratch(c, SL_V_COST1, ne * 4, &c1v));
-            RTS_TRY(one_cost(c, p, p.cost1, p.aggr == RTS_AGGR_CROSS, H, W, v, (float *)c1v, SL_V_AUX));
-            if (p.cost2 != RTS_COST_NONE) {
-                void *c2v;
-                RTS_TRY(scratch(c, SL_V_COST2, ne * 4, &c2v));
-                RTS_TRY(one_cost(c, p, p.cost2, false, H, W, v, (float *)c2v, SL_TMP2));
-                const float *l1, *l2;
-                RTS_TRY(combine_luts(c, p.lambda1, p.lambda2, &l1, &l2));
-                launch_combine(s, (float *)c1v, (const float *)c2v, (long)ne, l1, l2, p.lambda1, p.lambda2);
-                count_launch(c);
-            }
+            RTS_TRY(cost_volume_composed(c, p, H, W, v, (float *)c1v));
         }
         vol = c1v;
     }
-    if (p.aggr == RTS_AGGR_CROSS) {
-        RTS_TRY(cross_fused(c, p, H, W, rr, rt, ar, at, (const float *)vol, (uint16_t *)raw, (int *)rl));
-    } else {
-        RTS_TRY(aw_fused(c, p, H, W, vol, vol_half, v.lref, v.ltar, (uint16_t *)raw, (int *)rl, nullptr));
-    }
+    RTS_TRY(aw_fused(c, p, H, W, vol, vol_half, v.lref, v.ltar, (uint16_t *)raw, (int *)rl, nullptr));
     {
         StageScope sc(c, "wta_fill");
         launch_wta_fill(s, (const uint16_t *)raw, (const int *)rl, disp, H, W, mirror);
@@ -252,8 +254,66 @@ static rts_status view_fused(rts_ctx *c, const rts_params &p, int H, int W, cons
 
 rts_status run_view(rts_ctx *c, const rts_params &p, int H, int W, const ViewIn &v, uint8_t *disp, int mirror,
                     float *cost_out) {
-    if (!cost_out && fused_supported(p, H, W)) return view_fused(c, p, H, W, v, disp, mirror);
+    if (!cost_out && p.aggr == RTS_AGGR_AW && fused_supported(p, H, W)) return view_fused(c, p, H, W, v, disp, mirror);
     return view_composed(c, p, H, W, v, disp, mirror, cost_out);
+}
+
+// Cross-based pipeline of one pair over a view table: both views run in the
+// same launch of every stage (the right view through mirrored addressing).
+static rts_status pipeline_cross_views(rts_ctx *c, const rts_params &p, int H, int W, const uint8_t *lg,
+                                       const uint8_t *rg, const uint8_t *lc, const uint8_t *rc, uint8_t *dl,
+                                       uint8_t *dr, uint8_t *mask) {
+    if (fast_costs(p)) {
+        // the batched form with one pair: autotuned tiles and a captured graph per shape
+        rts_pair pr{W, H, lg, rg, lc, rc, nullptr, nullptr};
+        rts_out o{dl, dr, mask, nullptr};
+        return batch_views_run(c, 1, &pr, &p, &o);
+    }
+    const int nv = p.right_view ? 2 : 1;
+    const int half = p.precision == RTS_PREC_F16 ? 1 : 0;
+    const int Ws[2] = {W, W}, Hs[2] = {H, H}, Ds[2] = {p.disp_range, p.disp_range};
+    CrossTune tune;
+    ViewBatch b;
+    RTS_TRY(plan_views(c, SL_BATCH0, Ws, Hs, Ds, nv, half, tune, &b));
+    ViewDesc &v0 = b.views[0];
+    v0.gref = lg; v0.gtar = rg; v0.cref = lc; v0.ctar = rc; v0.mirror = 0; v0.disp = dl;
+    if (nv == 2) {
+        ViewDesc &v1 = b.views[1];
+        v1.gref = rg; v1.gtar = lg; v1.cref = rc; v1.ctar = lc; v1.mirror = 1; v1.disp = dr;
+        v0.mask = mask;
+        v0.partner = 1;
+    }
+    int has_vol = 0;
+    if (!fast_costs(p)) {
+        // other costs: the module kernels build each view's volume first
+        // (the right view from mirrored copies of the images)
+        has_vol = 1;
+        const size_t np = (size_t)H * W, ne = np * p.disp_range;
+        StageScope sc(c, "cost");
+        void *vol0;
+        RTS_TRY(scratch(c, SL_BATCH2, ne * 4, &vol0));
+        ViewIn in0{lg, rg, lc, rc, nullptr, nullptr};
+        RTS_TRY(cost_volume_composed(c, p, H, W, in0, (float *)vol0));
+        b.views[0].vol = (const float *)vol0;
+        if (nv == 2) {
+            void *gv, *cv, *vol1;
+            RTS_TRY(scratch(c, SL_V_GRAY, np * 2, &gv));
+            RTS_TRY(scratch(c, SL_V_LAB, np * 6, &cv));
+            uint8_t *fg_r = (uint8_t *)gv, *fg_l = fg_r + np, *fc_r = (uint8_t *)cv, *fc_l = fc_r + 3 * np;
+            launch_flip(c->stream, rg, fg_r, H, W, 1, 1);
+            launch_flip(c->stream, lg, fg_l, H, W, 1, 1);
+            launch_flip(c->stream, rc, fc_r, H, W, 3, 1);
+            launch_flip(c->stream, lc, fc_l, H, W, 3, 1);
+            count_launch(c, 4);
+            RTS_TRY(scratch(c, SL_BATCH3, ne * 4, &vol1));
+            ViewIn in1{fg_r, fg_l, fc_r, fc_l, nullptr, nullptr};
+            RTS_TRY(cost_volume_composed(c, p, H, W, in1, (float *)vol1));
+            b.views[1].vol = (const float *)vol1;
+        }
+    }
+    ViewTable t;
+    RTS_TRY(upload_views(c, b, tune, nullptr, &t));
+    return launch_cross_views(c, p, t, half, has_vol, b.max_d, tune, b.row_last_all, b.row_last_count);
 }
 
 // Prepares device inputs for both views and runs them; all pointers device.
@@ -276,6 +336,8 @@ rts_status pipeline_device(rts_ctx *c, const rts_params &p, int H, int W, const 
         lc = a;
         rc = b;
     }
+    if (!cost_out && p.aggr == RTS_AGGR_CROSS && cross_fused_supported(p))
+        return pipeline_cross_views(c, p, H, W, lg, rg, lc, rc, dl, dr, mask);
     {
         StageScope sc(c, "left_view");
         ViewIn v{lg, rg, lc, rc, ll, rl};

@@ -1,0 +1,104 @@
+"""Batched form (rts_batch_run: one launch per stage for all pairs, CUDA graph
+replay, autotuned tiles) and the serving loop (rts_server_*): every pair's
+result is the same as its single-pair pipeline run -- alone and in the mix --
+and the single-pair run is pinned to the oracle elsewhere."""
+import numpy as np
+import pytest
+
+from conftest import bits_equal
+
+pytestmark = pytest.mark.gpu
+
+MIX = [(160, 120, 32), (96, 64, 64), (200, 90, 16), (128, 128, 128), (64, 48, 32), (250, 60, 64)]
+
+
+def make_pairs(seed0):
+    import rtstereo_gb300 as R
+    out = []
+    for i, (W, H, D) in enumerate(MIX):
+        L, Rr, _ = R.synth_pair(seed0 + i, W, H, D, 4, 1, 2.0, min(4, D - 1))
+        out.append((L, Rr, D))
+    return out
+
+
+def single(ctx, L, Rr, D, prec):
+    import rtstereo_gb300 as R
+    return ctx.pipeline(R.params(disp_range=D, precision=prec), L, Rr)[:3]
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_batch_matches_single_runs(ctx, oracle_mod, prec):
+    torch = pytest.importorskip("torch")
+    import rtstereo_gb300 as R
+    s = torch.cuda.Stream()
+    ctx.set_stream(s.cuda_stream)
+    try:
+        for rnd in range(2):  # the second round replays the captured graph with new data
+            data = make_pairs(1000 * rnd + 7)
+            dev, pairs, params, outs, bufs = [], [], [], [], []
+            for L, Rr, D in data:
+                H, W = L.shape
+                dl, dr = torch.from_numpy(L).cuda(), torch.from_numpy(Rr).cuda()
+                o = [torch.zeros((H, W), dtype=torch.uint8, device="cuda") for _ in range(3)]
+                dev.append((dl, dr))
+                bufs.append(o)
+                pairs.append(R.Pair(W, H, dl.data_ptr(), dr.data_ptr(), None, None, None, None))
+                params.append(R.params(disp_range=D, precision=prec))
+                outs.append(R.Out(o[0].data_ptr(), o[1].data_ptr(), o[2].data_ptr(), None))
+            s.wait_stream(torch.cuda.current_stream())
+            ctx.batch_run(pairs, params, outs)
+            s.synchronize()
+            for (L, Rr, D), o in zip(data, bufs):
+                want = single(ctx, L, Rr, D, prec)
+                for g, w in zip(o, want):
+                    assert bits_equal(g.cpu().numpy(), w)
+    finally:
+        ctx.set_stream(None)
+    # and the plain single-pair run itself equals the oracle for one of them
+    if prec == 0:
+        L, Rr, D = make_pairs(7)[0]
+        O = oracle_mod
+        rgb = lambda a: np.ascontiguousarray(np.repeat(a[:, :, None], 3, axis=2))
+        o = O.pipeline(O.params(D=D), L, Rr, rgb(L), rgb(Rr))
+        g = single(ctx, L, Rr, D, 0)
+        assert all(bits_equal(a, b) for a, b in zip(g, o[:3]))
+
+
+def test_server_same_alone_and_in_the_mix(ctx):
+    import rtstereo_gb300 as R
+    srv = R.Server(ctx, hbm_budget=1 << 30, max_inflight=8, max_batch=3, precision=R.PREC_F16)
+    try:
+        data = make_pairs(55) * 3
+        tickets = []
+        for L, Rr, D in data:
+            tickets.append(srv.submit(R.params(disp_range=D, precision=R.PREC_F16), L, Rr))
+            srv.progress()
+        stats = [srv.wait(t) for t, _ in tickets]
+        for (L, Rr, D), (t, outs) in zip(data, tickets):
+            want = single(ctx, L, Rr, D, R.PREC_F16)
+            for g, w in zip(outs, want):
+                assert bits_equal(g, w)
+        assert all(s[0] <= s[1] <= s[2] for s in stats)
+    finally:
+        srv.close()
+
+
+def test_server_admission_and_cancel(ctx):
+    import rtstereo_gb300 as R
+    # a small budget: a large request is refused outright, small ones queue for memory
+    srv = R.Server(ctx, hbm_budget=24 << 20, max_inflight=2, max_batch=1, precision=R.PREC_F16)
+    try:
+        L, Rr, _ = R.synth_pair(3, 1024, 768, 128, 4, 0, 2.0, 4)
+        with pytest.raises(R.RtsError) as e:
+            srv.submit(R.params(disp_range=128, precision=R.PREC_F16), L, Rr)
+        assert e.value.status == 6  # RTS_ERR_BUSY: larger than the server's HBM budget
+        data = make_pairs(9)[:5]
+        tickets = [srv.submit(R.params(disp_range=D, precision=R.PREC_F16), a, b)[0] for a, b, D in data]
+        assert srv.cancel(tickets[-1]) == 0
+        for t in tickets[:-1]:
+            srv.wait(t)
+        with pytest.raises(R.RtsError) as e:
+            srv.wait(tickets[-1])
+        assert e.value.status == 7  # RTS_ERR_CANCELLED
+    finally:
+        srv.close()
