@@ -75,8 +75,8 @@ __global__ void k_cost_volume(const uint4 *__restrict__ rr, const uint4 *__restr
 
 // ---------------------------------------------------------------------------
 // Adaptive-weight aggregation fused with the arg-min.  Block: one row y, 64
-// pixels x0..x0+63, all disparities in chunks of 64; 128 threads, each with
-// 8 pixels x 4 disparities.  Warp w owns pixels 16w..16w+15 for all 64
+// pixels x0..x0+63, all disparities in chunks of 64; 256 threads, each with
+// 4 pixels x 4 disparities.  Warp w owns pixels 8w..8w+7 for all 64
 // disparities (lane = 2 pixel groups x 16 disparity groups), so the reference
 // weights are broadcast loads and the target weights and costs are contiguous.
 // Per tap row ky the block stages the cost rows (wrapped columns x0-r ..
@@ -89,7 +89,7 @@ __global__ void k_cost_volume(const uint4 *__restrict__ rr, const uint4 *__restr
 // they are skipped.  A weight is pw[k] * G[|Lab(p)-Lab(q)|^2] with host tables
 // (seq/AdaptiveWeightAggregation.cpp:60-63); |Lab(p)-Lab(q)|^2 is the dot
 // product of the byte-wise absolute differences of the packed Lab words.
-constexpr int kAwTX = 64, kAwDC = 64, kAwThreads = 128;
+constexpr int kAwTX = 64, kAwDC = 64, kAwThreads = 256;
 constexpr int kAwCPitch = kAwDC + 4;
 constexpr uint32_t kLabOut = 0xff000000u;  // marks a column outside the image
 
@@ -106,7 +106,7 @@ __device__ __forceinline__ float lab_weight2(uint32_t c, uint32_t q, const float
 }
 
 template <typename CT, bool EXACT>
-__global__ void __launch_bounds__(kAwThreads) k_aw_wta(const CT *__restrict__ vol, const uint32_t *__restrict__ labr,
+__global__ void __launch_bounds__(kAwThreads, 3) k_aw_wta(const CT *__restrict__ vol, const uint32_t *__restrict__ labr,
                                                       const uint32_t *__restrict__ labt, const float *__restrict__ pw,
                                                       const float *__restrict__ G, uint16_t *__restrict__ raw,
                                                       int *__restrict__ row_last, float *__restrict__ cost_out, int H,
@@ -126,7 +126,7 @@ __global__ void __launch_bounds__(kAwThreads) k_aw_wta(const CT *__restrict__ vo
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int td = lane & 15;                      // disparities 4td .. 4td+3 of the chunk
-    const int px0 = 16 * warp + 8 * (lane >> 4);  // pixels px0 .. px0+7 of the tile
+    const int px0 = 8 * warp + 4 * (lane >> 4);  // pixels px0 .. px0+3 of the tile
     const int y = blockIdx.y, x0 = blockIdx.x * kAwTX;
     if (tid < kAwTX) {
         best_v[tid] = __int_as_float(0x7f800000);
@@ -135,9 +135,9 @@ __global__ void __launch_bounds__(kAwThreads) k_aw_wta(const CT *__restrict__ vo
     const bool vec = (D & 3) == 0;
 
     for (int dc0 = 0; dc0 < D; dc0 += kAwDC) {
-        float sw[8][4], sc[8][4];
+        float sw[4][4], sc[4][4];
 #pragma unroll
-        for (int j = 0; j < 8; j++)
+        for (int j = 0; j < 4; j++)
 #pragma unroll
             for (int i = 0; i < 4; i++) sw[j][i] = sc[j][i] = 0.f;
         // centre Lab words: reference pixels x0+lane+32m, target columns t(u), u = lane+32m
@@ -226,14 +226,14 @@ __global__ void __launch_bounds__(kAwThreads) k_aw_wta(const CT *__restrict__ vo
             // u index of wT for (j, i): px0 + j - 4td - i + 63 = ubase + (j - i) + 3
             const int ubase = px0 - 4 * td + kAwDC - 4;
             const float *cbase = Cs + px0 * kAwCPitch + 4 * td;
-            // taps in groups of 4: the 11 cost columns px0+kx0 .. px0+kx0+10 of a group
-            // are loaded once and serve 8 pixels x 4 taps
+            // taps in groups of 4: the 7 cost columns px0+kx0 .. px0+kx0+6 of a group
+            // are loaded once and serve 4 pixels x 4 taps
 #pragma unroll 1
             for (int kx0 = 0; kx0 < e; kx0 += 4) {
                 const int g = imin(4, e - kx0);
-                float cw[11][4];
+                float cw[7][4];
 #pragma unroll
-                for (int q = 0; q < 11; q++) {
+                for (int q = 0; q < 7; q++) {
                     const float4 v = *reinterpret_cast<const float4 *>(cbase + (kx0 + q) * kAwCPitch);
                     cw[q][0] = v.x; cw[q][1] = v.y; cw[q][2] = v.z; cw[q][3] = v.w;
                 }
@@ -241,18 +241,15 @@ __global__ void __launch_bounds__(kAwThreads) k_aw_wta(const CT *__restrict__ vo
                 for (int u = 0; u < 4; u++) {
                     if (u < g) {
                         const int kx = kx0 + u;
-                        float wr[8], wt[11];
+                        float wr[4], wt[7];
                         const float4 a0 = *reinterpret_cast<const float4 *>(wRs + kx * kAwTX + px0);
-                        const float4 a1 = *reinterpret_cast<const float4 *>(wRs + kx * kAwTX + px0 + 4);
                         wr[0] = a0.x; wr[1] = a0.y; wr[2] = a0.z; wr[3] = a0.w;
-                        wr[4] = a1.x; wr[5] = a1.y; wr[6] = a1.z; wr[7] = a1.w;
                         const float4 *wp = reinterpret_cast<const float4 *>(wTs + kx * NTP + ubase);
-                        const float4 b0 = wp[0], b1 = wp[1], b2 = wp[2];
+                        const float4 b0 = wp[0], b1 = wp[1];
                         wt[0] = b0.x; wt[1] = b0.y; wt[2] = b0.z; wt[3] = b0.w;
-                        wt[4] = b1.x; wt[5] = b1.y; wt[6] = b1.z; wt[7] = b1.w;
-                        wt[8] = b2.x; wt[9] = b2.y; wt[10] = b2.z;
+                        wt[4] = b1.x; wt[5] = b1.y; wt[6] = b1.z;
 #pragma unroll
-                        for (int j = 0; j < 8; j++)
+                        for (int j = 0; j < 4; j++)
 #pragma unroll
                             for (int i = 0; i < 4; i++) {
                                 const float w = __fmul_rn(wr[j], wt[j - i + 3]);
@@ -268,7 +265,7 @@ __global__ void __launch_bounds__(kAwThreads) k_aw_wta(const CT *__restrict__ vo
         // score / sum of weights (seq/AdaptiveWeightAggregation.cpp:108), staged for the arg-min
         float *outs = Cs;  // [64][kAwDC + 1]
 #pragma unroll
-        for (int j = 0; j < 8; j++)
+        for (int j = 0; j < 4; j++)
 #pragma unroll
             for (int i = 0; i < 4; i++) {
                 const float v = __fdiv_rn(sc[j][i], sw[j][i]);
