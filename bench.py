@@ -324,13 +324,17 @@ def run_ours(args, rank, world):
     torch.cuda.set_stream(stream)
     ctx.set_stream(stream.cuda_stream)
 
-    # device-resident inputs and outputs
+    # device-resident inputs and outputs; a pipeline gets the images it reads:
+    # the cross-based one gray images only (colour = gray in three channels, as the
+    # reference driver reads a gray file), adaptive weights also RGB and Lab
+    gray_only = ag == 3
     t = lambda a: torch.from_numpy(a).to(f"cuda:{dev}")
     dL, dR, dLc, dRc, dLl, dRl = (t(a) for a in (L, Rr, Lc, Rc, Ll, Rl))
+    ptr = lambda a: None if gray_only else a.data_ptr()
     o_dl = torch.empty((H, W), dtype=torch.uint8, device=f"cuda:{dev}")
     o_dr = torch.empty_like(o_dl)
     o_mk = torch.empty_like(o_dl)
-    pair = R.Pair(W, H, dL.data_ptr(), dR.data_ptr(), dLc.data_ptr(), dRc.data_ptr(), dLl.data_ptr(), dRl.data_ptr())
+    pair = R.Pair(W, H, dL.data_ptr(), dR.data_ptr(), ptr(dLc), ptr(dRc), ptr(dLl), ptr(dRl))
     out = R.Out(o_dl.data_ptr(), o_dr.data_ptr(), o_mk.data_ptr(), None)
     import ctypes as C
     lib = R.lib()
@@ -384,7 +388,7 @@ def run_ours(args, rank, world):
     pin = lambda a: torch.from_numpy(a).pin_memory()
     hL, hR, hLc, hRc, hLl, hRl = (pin(a) for a in (L, Rr, Lc, Rc, Ll, Rl))
     ho = [torch.empty((H, W), dtype=torch.uint8).pin_memory() for _ in range(3)]
-    hpair = R.Pair(W, H, hL.data_ptr(), hR.data_ptr(), hLc.data_ptr(), hRc.data_ptr(), hLl.data_ptr(), hRl.data_ptr())
+    hpair = R.Pair(W, H, hL.data_ptr(), hR.data_ptr(), ptr(hLc), ptr(hRc), ptr(hLl), ptr(hRl))
     hout = R.Out(ho[0].data_ptr(), ho[1].data_ptr(), ho[2].data_ptr(), None)
 
     def hstep():
@@ -404,7 +408,7 @@ def run_ours(args, rank, world):
         tt = torch.tensor([e2e_ms], device=f"cuda:{dev}")
         torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
         e2e_ms = float(tt.item())
-    h2d = sum(a.numel() for a in (hL, hR, hLc, hRc, hLl, hRl))
+    h2d = sum(a.numel() for a in ((hL, hR) if gray_only else (hL, hR, hLc, hRc, hLl, hRl)))
     d2h = 3 * W * H
 
     # parity spot check of this run's output against the last device run

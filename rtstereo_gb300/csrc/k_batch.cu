@@ -2,19 +2,29 @@
 // stage for a whole batch (one pair = its left and right view).
 //
 // Stages (each a persistent kernel looping over the work items of all views):
-//   prep   block per (view, image, row): 16-byte pixel records of the view's
-//          reference and target image (census code, packed RGB, packed arms),
-//          read through mirrored addressing for right views
+//   prep   block per (image, 64x16 tile): per-pixel records of every image
+//          (census code, colour, horizontal arms) and arm words (horizontal and
+//          vertical arms), in image coordinates, made once per image and read by
+//          both views of the pair
 //   hseg   warp per (view, row, 32 disparities): cost, running sum along x
-//          (seq/CrossBasedAggregation.cpp:117-125), row segments (:151-160) and
-//          the geometry word of every entry
-//   vert   block per (view, column, 64-row strip): vertical sums of the row
-//          segments over the cross (:140-167), the division, and the first strict
-//          arg-min over d (seq/WTA.cpp:15-22)
+//          (seq/CrossBasedAggregation.cpp:117-125) and the row segment of every
+//          entry (:151-160)
+//   vert   block per (view, column, strip of rows): row segments streamed down
+//          the column through a shared ring, vertical sums over the cross
+//          (:140-167), the division and the first strict arg-min over d
+//          (seq/WTA.cpp:15-22)
 //   fill   warp per (view, row): the winner carry of seq/WTA.cpp:12
 //   cc     block per (pair, row): seq/CrossCheck.cpp:10-23
-// The per-entry arithmetic is the reference's (see k_pipe.cu), so a pair's
-// result does not depend on what else is in the batch.
+//
+// A right view is the left-to-right pipeline on the mirrored images.  It reads
+// the pair's records through mirrored column addressing with the left and right
+// arms swapped; its census codes are the unmirrored ones, which differ from the
+// codes of the mirrored image only by one fixed permutation of the bits (the
+// window, and its wrap at the borders, are mirror symmetric), so every Hamming
+// distance is the same.  The per-entry arithmetic is the reference's, so a
+// pair's result does not depend on what else is in the batch.
+#include <type_traits>
+
 #include "rts_fused.cuh"
 #include "rts_views.h"
 
@@ -31,344 +41,497 @@ __device__ __forceinline__ int find_view(const int *__restrict__ off, int n, int
 }
 
 // ---------------------------------------------------------------------------
-// prep: block per (view, image, row, 128-column segment).  The block stages in
-// shared memory, in view coordinates (mirrored for right views): the census
-// rows y-hr .. y+hr for columns x0-wr .. x0+127+wr (wrapped, as the census
-// wraps, seq/CensusTransform.cpp:20-26), the packed colours of row y for
-// columns x0-L .. x0+127+L and of rows y-L .. y+L for columns x0 .. x0+127
-// (arms stop at the image edge, so those are not wrapped).
-constexpr int kPrepSeg = 128;
+// prep: block per (view, image, 64x16 tile).  The colours of the tile and of
+// L pixels around it (no wrap: arms stop at the image edge) and the gray census
+// window around it (wrapped, seq/CensusTransform.cpp:20-26) are staged in
+// shared memory; each thread then makes four pixels.
+constexpr int kPrepTW = 64, kPrepTH = 16, kPrepT = 256;
 constexpr uint32_t kNoPixel = 0xff000000u;
 
-__global__ void __launch_bounds__(kPrepSeg) k_prep_views(ViewTable t, int hr, int wr, int L, int tau, int want_code) {
+static size_t prep_smem(int hr, int wr, int L) {
+    return (size_t)4 * (kPrepTW + 2 * L) * (kPrepTH + 2 * L) + (size_t)(kPrepTH + 2 * hr) * (kPrepTW + 2 * wr);
+}
+
+// GRAYREC: the record colour is the gray byte (all views of the launch are
+// gray; the cost kernel then takes 3|dI| as the colour AD), else packed RGB with
+// gray replicated into the three channels (seq/Main.cpp:87-90)
+template <int GRAYREC>
+__global__ void __launch_bounds__(kPrepT) k_prep_views(ViewTable t, int hr, int wr, int L, int tau, int want_code) {
     extern __shared__ __align__(16) unsigned char psm[];
     const int nv = t.nviews;
     const int *off = t.off + ST_PREP * (nv + 1);
-    const int cw = kPrepSeg + 2 * wr;           // census tile width
-    const int hw = kPrepSeg + 2 * L;            // horizontal colour row
-    uint8_t *ct = psm;                          // [(2hr+1)][cw]
-    uint32_t *hrow = reinterpret_cast<uint32_t *>(psm + (((2 * hr + 1) * cw + 15) & ~15));  // [hw]
-    uint32_t *vcol = hrow + hw;                 // [(2L+1)][kPrepSeg]
-    const int tx = threadIdx.x;
+    const int cw = kPrepTW + 2 * L, chh = kPrepTH + 2 * L;
+    const int gw = kPrepTW + 2 * wr, gh = kPrepTH + 2 * hr;
+    uint32_t *ct = reinterpret_cast<uint32_t *>(psm);  // [chh][cw] colours
+    uint8_t *gt = psm + (size_t)4 * cw * chh;          // [gh][gw] gray, wrapped
     for (int item = blockIdx.x; item < t.total[ST_PREP]; item += gridDim.x) {
         const int v = find_view(off, nv, item);
         const ViewDesc &V = t.views[v];
-        const int W = V.W, H = V.H, mir = V.mirror;
-        const int nseg = (W + kPrepSeg - 1) / kPrepSeg;
+        const int W = V.W, H = V.H;
+        const int ntx = (W + kPrepTW - 1) / kPrepTW, nty = (H + kPrepTH - 1) / kPrepTH;
         const int local = item - __ldg(off + v);
-        const int img = local >= H * nseg ? 1 : 0;
-        const int rest = local - img * H * nseg;
-        const int y = rest / nseg, x0 = (rest - y * nseg) * kPrepSeg;
+        const int img = local >= ntx * nty ? 1 : 0;
+        const int tl = local - img * ntx * nty;
+        const int by = tl / ntx;
+        const int x0 = (tl - by * ntx) * kPrepTW, y0 = by * kPrepTH;
         const uint8_t *gray = img ? V.gtar : V.gref;
         const uint8_t *rgb = img ? V.ctar : V.cref;
-        uint4 *out = img ? V.rtar : V.rref;
-        auto sx = [&](int xm) { return mir ? W - 1 - xm : xm; };
-        // colour of a pixel in view coordinates; without an RGB image the gray value
-        // in all three channels (what the reference driver reads from a gray file,
-        // seq/Main.cpp:87-90)
-        auto colour = [&](int qy, int qx) -> uint32_t {
-            if (qx < 0 || qx >= W || qy < 0 || qy >= H) return kNoPixel;
-            const size_t q = (size_t)qy * W + sx(qx);
-            if (!rgb) return (uint32_t)gray[q] * 0x010101u;
-            const uint8_t *px = rgb + 3 * q;
-            return (uint32_t)px[0] | ((uint32_t)px[1] << 8) | ((uint32_t)px[2] << 16);
-        };
+        uint4 *rec = img ? V.rtar : V.rref;
+        uint2 *arm = img ? V.atar : V.aref;
         __syncthreads();  // previous item done with the tiles
-        if (want_code)
-            for (int q = tx; q < (2 * hr + 1) * cw; q += kPrepSeg) {
-                const int r = q / cw, cx = q - r * cw;
-                const int yy = wrap1(y - hr + r, H);
-                const int xx = x0 - wr + cx;
-                // columns past the end of the last segment are never read by real pixels
-                const int xw = imin(imax(wrap1(xx, W), 0), W - 1);
-                ct[q] = gray[(size_t)yy * W + sx(xw)];
+        for (int q = threadIdx.x; q < cw * chh; q += kPrepT) {
+            const int r = q / cw, cx = q - r * cw;
+            const int yy = y0 - L + r, xx = x0 - L + cx;
+            uint32_t col = kNoPixel;
+            if (yy >= 0 && yy < H && xx >= 0 && xx < W) {
+                const size_t p = (size_t)yy * W + xx;
+                if (!rgb) {
+                    col = gray[p];
+                    if (!GRAYREC) col *= 0x010101u;
+                } else {
+                    const uint8_t *px = rgb + 3 * p;
+                    col = (uint32_t)px[0] | ((uint32_t)px[1] << 8) | ((uint32_t)px[2] << 16);
+                }
             }
-        for (int q = tx; q < hw; q += kPrepSeg) hrow[q] = colour(y, x0 - L + q);
-        for (int q = tx; q < (2 * L + 1) * kPrepSeg; q += kPrepSeg) {
-            const int r = q / kPrepSeg, cx = q - r * kPrepSeg;
-            vcol[q] = colour(y - L + r, x0 + cx);
+            ct[q] = col;
         }
+        if (want_code)
+            for (int q = threadIdx.x; q < gw * gh; q += kPrepT) {
+                const int r = q / gw, cx = q - r * gw;
+                // rows / columns past the last pixel's window are never read; clamp them
+                // into the single-wrap range (hr < H, wr < W)
+                const int yy = wrap1(imin(y0 - hr + r, H - 1 + hr), H);
+                const int xx = wrap1(imin(x0 - wr + cx, W - 1 + wr), W);
+                gt[q] = gray[(size_t)yy * W + xx];
+            }
         __syncthreads();
-        const int x = x0 + tx;
-        if (x < W) {
-            uint64_t code = 0;
+        const int px = threadIdx.x & (kPrepTW - 1);
+        for (int py = threadIdx.x / kPrepTW; py < kPrepTH; py += kPrepT / kPrepTW) {
+            const int x = x0 + px, y = y0 + py;
+            if (x >= W || y >= H) continue;
+            uint32_t lo = 0, hi = 0;
             if (want_code) {
-                const uint8_t c = ct[hr * cw + wr + tx];
+                // seq/CensusTransform.cpp:11-37: bit (dy+hr)*(2wr+1)+(dx+wr), strict centre > neighbour
+                const uint8_t *g0 = gt + py * gw + px;
+                const uint32_t c = g0[hr * gw + wr];
                 int k = 0;
                 for (int r = 0; r <= 2 * hr; r++)
-                    for (int dx = 0; dx <= 2 * wr; dx++, k++) code |= (uint64_t)(c > ct[r * cw + tx + dx]) << k;
+                    for (int dx = 0; dx <= 2 * wr; dx++, k++) {
+                        const uint32_t bit = c > (uint32_t)g0[r * gw + dx] ? 1u : 0u;
+                        if (k < 32) lo |= bit << k;
+                        else hi |= bit << (k - 32);
+                    }
             }
-            const uint32_t packed = hrow[L + tx];
             // cross arms, seq/CrossBasedAggregation.cpp:12-100: step while the max channel
-            // difference to the centre stays below tau and the arm is shorter than L;
-            // the first failing pixel is included; stop at the image edge
-            auto delta = [&](uint32_t q) {
-                const uint32_t ad = __vabsdiffu4(packed, q);
+            // difference to the centre stays below tau and the arm is shorter than L; the
+            // first failing pixel is included; stop at the image edge
+            const uint32_t *cc = ct + (py + L) * cw + (px + L);
+            const uint32_t centre = *cc;
+            auto delta = [&](uint32_t q) -> int {
+                if (GRAYREC) return abs((int)q - (int)centre);
+                const uint32_t ad = __vabsdiffu4(centre, q);
                 return imax(imax((int)(ad & 0xff), (int)((ad >> 8) & 0xff)), (int)((ad >> 16) & 0xff));
             };
-            int len[4];
             const int room[4] = {x, W - 1 - x, y, H - 1 - y};
+            const int stride[4] = {-1, 1, -cw, cw};
+            int len[4];
 #pragma unroll
             for (int a = 0; a < 4; a++) {
                 int n = 0, dl = 0;
                 while (dl < tau && n < L && n < room[a]) {
                     n++;
-                    const uint32_t q = a == 0 ? hrow[L + tx - n] : a == 1 ? hrow[L + tx + n]
-                                     : a == 2 ? vcol[(L - n) * kPrepSeg + tx] : vcol[(L + n) * kPrepSeg + tx];
-                    dl = delta(q);
+                    dl = delta(cc[stride[a] * n]);
                 }
                 len[a] = n;
             }
-            const uint32_t arms = (uint32_t)len[0] | ((uint32_t)len[1] << 8) | ((uint32_t)len[2] << 16) |
-                                  ((uint32_t)len[3] << 24);
-            out[(size_t)y * W + x] = make_uint4((uint32_t)code, (uint32_t)(code >> 32), packed, arms);
+            const uint32_t lr = (uint32_t)len[0] | ((uint32_t)len[1] << 16);
+            const uint32_t tb = (uint32_t)len[2] | ((uint32_t)len[3] << 16);
+            const size_t p = (size_t)y * W + x;
+            rec[p] = make_uint4(lo, hi, centre, lr);
+            arm[p] = make_uint2(lr, tb);
         }
     }
 }
 
 // ---------------------------------------------------------------------------
-// hseg: lane = disparity; 16-column steps of cost + running sum into registers,
-// then a 64-entry ring per lane in shared memory and the segments whose right
-// end is known (arms <= 23).  Records are staged 32 columns at a time.
-constexpr int kRingV = 64;
-constexpr int kHsegW = 2;
-constexpr int kStepV = 16;
+// hseg: lane = disparity.  The running sum P of every column goes into a
+// 64-column ring per lane; the segment of column xs is written 24 columns
+// later (arms <= 23, so both of its ends are in the ring then):
+//   seg(xs) = P[xs + r] - P[max(xs - l - 1, 0)]
+// with (l, r) the byte-wise minimum of the reference and target arms kept in a
+// 32-column ring as the pre-shifted word (l + 1) << 7 | r << 23.  Records are
+// staged 32 columns at a time and worked in groups of kHSub columns: the costs
+// (independent), the running sum, the segments of the columns 24 back, then
+// the arm words.  Columns past the row end are computed from clamped records
+// and never written.
+constexpr int kHsegW = 2;   // warps per block
+constexpr int kHLag = 24;   // columns between a column's prefix and its segment
+constexpr int kHSub = 8;    // columns per group
 
-// MODE: 0 precomputed volume, 1 truncated AD + census on the integer path (the
-// configuration of the cross-based pipeline), 2 any AD/census combination
-template <typename ST, int MODE>
-__global__ void __launch_bounds__(kHsegW * 32) k_hseg_views(ViewTable t, CostCfg cfg, int L) {
-    constexpr bool VOL = MODE == 0;
-    __shared__ float pring[kHsegW][kRingV][32];
-    __shared__ uint16_t lring[kHsegW][kRingV][32];
+// MODE: 0 precomputed volume, 1 truncated AD + census through the combined host
+// table (the configuration of the cross-based pipeline), 2 any AD/census pair
+template <typename ST, int MODE, int GRAYREC>
+__global__ void __launch_bounds__(kHsegW * 32, 8) k_hseg_views(ViewTable t, CostCfg cfg, const float *__restrict__ lut2d) {
+    __shared__ __align__(16) float pring[kHsegW][64][32];
+    __shared__ uint32_t lring[kHsegW][32][32];
     __shared__ uint4 recA[kHsegW][32];
     __shared__ uint4 recB[kHsegW][64];
-    __shared__ float volS[VOL ? kHsegW : 1][VOL ? 32 : 1][33];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int nv = t.nviews;
     const int *off = t.off + ST_HSEG * (nv + 1);
-    float (*P)[32] = pring[warp];
-    uint16_t (*LR)[32] = lring[warp];
+    float *PR = &pring[warp][0][lane];  // slot s at PR[32 s]
+    uint32_t *LR = &lring[warp][0][lane];
     uint4 *RA = recA[warp], *RB = recB[warp];
     for (int item = blockIdx.x * kHsegW + warp; item < t.total[ST_HSEG]; item += gridDim.x * kHsegW) {
         const int v = find_view(off, nv, item);
         const ViewDesc &V = t.views[v];
-        const int W = V.W, D = V.D;
+        const int W = V.W, D = V.D, mir = V.mirror;
         const int nch = (D + 31) >> 5;
         const int local = item - __ldg(off + v);
         const int y = local / nch, dbase = (local - y * nch) * 32;
         const int d = dbase + lane;
         const bool active = d < D;
         const int dd = active ? d : D - 1;
-        const int lo = dd - dbase;
         const size_t row = (size_t)y * W;
-        const uint4 *rr = V.rref, *rt = V.rtar;
-        ST *seg = reinterpret_cast<ST *>(V.seg);
-        uint16_t *geo = V.geo;
-        const float *vol = V.vol;
-
-        auto emit = [&](int xs) {
-            const uint16_t lr = LR[xs & (kRingV - 1)][lane];
-            const int l = lr & 0xff, r = lr >> 8;
-            int xl = xs - l - 1;
-            if (xl < 0) xl = 0;  // seq/CrossBasedAggregation.cpp:153-154
-            const int xr = xs + r;
-            const float s = __fsub_rn(P[xr & (kRingV - 1)][lane], P[xl & (kRingV - 1)][lane]);
-            if (active) seg[(row + xs) * D + d] = to_store<ST>(s);
+        const uint4 *rr = V.rref + row, *rt = V.rtar + row;
+        ST *seg = reinterpret_cast<ST *>(V.seg) + row * D + d;
+        const float *vol = MODE == 0 ? V.vol + row * D + dd : nullptr;
+        // image column of view column xv (any integer: columns past the row end wrap)
+        auto col = [&](int xv) {
+            xv %= W;
+            if (xv < 0) xv += W;
+            return mir ? W - 1 - xv : xv;
         };
-        auto wrapx = [&](int tt) {
-            tt %= W;
-            return tt < 0 ? tt + W : tt;
+        // a mirrored view swaps the left and right arms
+        auto fix = [&](uint4 r) {
+            if (mir) r.w = __byte_perm(r.w, 0, 0x1032);
+            return r;
         };
         uint4 na, nb0, nb1;
         auto fetch = [&](int x0) {
-            const int t0 = x0 - dbase - 31;
-            na = rr[row + imin(x0 + lane, W - 1)];
-            nb0 = rt[row + wrapx(t0 + lane)];
-            nb1 = rt[row + wrapx(t0 + 32 + lane)];
+            const int t0 = x0 - dbase - 31;  // target column of RB[0]: x - d for x = x0, lane 31
+            na = rr[col(imin(x0 + lane, W - 1))];
+            nb0 = rt[col(t0 + lane)];
+            nb1 = rt[col(t0 + 32 + lane)];
         };
         fetch(0);
         float acc = 0.f;
-        for (int x0 = 0; x0 < W; x0 += 32) {
+        const int xend = W + kHLag;
+        for (int x0 = 0; x0 < xend; x0 += 32) {
             __syncwarp();
-            RA[lane] = na;
-            RB[lane] = nb0;
-            RB[lane + 32] = nb1;
-            if constexpr (VOL) {
-#pragma unroll 8
-                for (int u = 0; u < 32; u++)
-                    if (x0 + u < W) volS[warp][u][lane] = vol[(row + x0 + u) * D + dd];
-            }
+            RA[lane] = fix(na);
+            RB[lane] = fix(nb0);
+            RB[lane + 32] = fix(nb1);
             __syncwarp();
-            if (x0 + 32 < W) fetch(x0 + 32);
-#pragma unroll 1
-            for (int h = 0; h < 32; h += kStepV) {
-                const int xb = x0 + h;
-                if (xb >= W) break;
-                const int n = imin(kStepV, W - xb);
-                float pv[kStepV];
-                uint16_t lv[kStepV];
+            if (x0 + 32 < xend) fetch(x0 + 32);
+            // group h: columns x0 + kHSub h .. x0 + kHSub (h + 1) - 1
+            auto group = [&](auto hc, auto edge) {
+                constexpr int h = decltype(hc)::value;
+                const int hx = x0 + kHSub * h;
+                float cv[kHSub];
+                uint32_t lv[kHSub];
 #pragma unroll
-                for (int u = 0; u < kStepV; u++) {
-                    if (u < n) {
-                        const uint4 a = RA[h + u];
-                        const uint4 b = RB[h + u + 31 - lo];  // target column x - dd
-                        float c;
-                        if constexpr (MODE == 0) {
-                            c = volS[warp][h + u][lane];
-                        } else if constexpr (MODE == 1) {
-                            // CombineCost of min(SAD, trunc) and the Hamming distance through
-                            // the host expf tables (seq/CombineCost.cpp:21-23)
-                            const int sad = imin((int)__vsadu4(a.z, b.z), cfg.itrunc);
-                            const int ham = __popc(a.x ^ b.x) + __popc(a.y ^ b.y);
-                            c = __fadd_rn(__ldg(cfg.lut1 + sad), __ldg(cfg.lut2 + ham));
-                        } else {
-                            c = pair_cost(a, b, cfg);
-                        }
-                        acc = (xb + u == 0) ? c : __fadd_rn(c, acc);  // seq/CrossBasedAggregation.cpp:123
-                        pv[u] = acc;
-                        const uint32_t m = __vminu4(a.w, b.w);  // byte-wise min of the four arms
-                        lv[u] = (uint16_t)(m & 0xffff);
-                        if (active)
-                            geo[(row + xb + u) * D + d] = (uint16_t)(((m & 0xff) + ((m >> 8) & 0xff) + 1) |
-                                                                     (((m >> 16) & 0xff) << 6) | ((m >> 24) << 11));
+                for (int u = 0; u < kHSub; u++) {
+                    const uint4 a = RA[kHSub * h + u];
+                    const uint4 b = RB[kHSub * h + u + 31 - lane];  // target column x - d
+                    if constexpr (MODE == 0) {
+                        cv[u] = vol[(size_t)imin(hx + u, W - 1) * D];
+                    } else if constexpr (MODE == 1) {
+                        // CombineCost of min(SAD, trunc) and the Hamming distance: one host-made
+                        // table of T1[s] + T2[h] (seq/CombineCost.cpp:21-23)
+                        int s = GRAYREC ? abs((int)a.z - (int)b.z) * 3 : (int)__vsadu4(a.z, b.z);
+                        s = imin(s, cfg.itrunc);
+                        const int hd = __popc(a.x ^ b.x) + __popc(a.y ^ b.y);
+                        cv[u] = __ldg(lut2d + s * 65 + hd);
+                    } else {
+                        cv[u] = pair_cost(a, b, cfg);
+                    }
+                    lv[u] = __vminu2(a.w, b.w) * 128u + 128u;
+                }
+                // running sum, seq/CrossBasedAggregation.cpp:123 (0 + c is c for every cost but -0)
+                float *PRh = PR + ((x0 & 32) + kHSub * h) * 32;
+#pragma unroll
+                for (int u = 0; u < kHSub; u++) {
+                    if constexpr (MODE == 0) acc = (hx + u == 0) ? cv[u] : __fadd_rn(acc, cv[u]);
+                    else acc = __fadd_rn(acc, cv[u]);
+                    PRh[u * 32] = acc;
+                }
+                // segments of columns xs = x - 24 (seq/CrossBasedAggregation.cpp:151-160; a left
+                // end before column 0 is clamped to column 0, :153-154)
+#pragma unroll
+                for (int u = 0; u < kHSub; u++) {
+                    const int xs = hx - kHLag + u;
+                    if (!decltype(edge)::value || (xs >= 0 && xs < W)) {
+                        const uint32_t e = LR[((kHSub * h + u - kHLag) & 31) * 32];
+                        const int xsl = xs << 7;
+                        const int il = imax(xsl - (int)(e & 0xffffu), 0);
+                        const int ir = xsl + (int)(e >> 16);
+                        // slot (column & 63) of the ring: the byte offset is (column << 7) & 0x1f80
+                        const float pl = PR[(il & 0x1f80) >> 2];
+                        const float pr = PR[(ir & 0x1f80) >> 2];
+                        if (active) seg[(size_t)xs * D] = to_store<ST>(__fsub_rn(pr, pl));
                     }
                 }
+                uint32_t *LRh = LR + kHSub * h * 32;
 #pragma unroll
-                for (int u = 0; u < kStepV; u++) {
-                    if (u < n) {
-                        P[(xb + u) & (kRingV - 1)][lane] = pv[u];
-                        LR[(xb + u) & (kRingV - 1)][lane] = lv[u];
-                    }
-                }
-                // segments whose right end xs + L is now in the ring
-#pragma unroll
-                for (int u = 0; u < kStepV; u++) {
-                    const int xs = xb - L + u;
-                    if (u < n && xs >= 0) emit(xs);
-                }
-            }
+                for (int u = 0; u < kHSub; u++) LRh[u * 32] = lv[u];
+            };
+            // a group whose segments are all inside the row needs no column checks
+            auto run = [&](auto hc) {
+                constexpr int h = decltype(hc)::value;
+                const int g0 = x0 + kHSub * h;
+                if (g0 >= kHLag && g0 + kHSub - 1 - kHLag < W) group(hc, std::false_type{});
+                else group(hc, std::true_type{});
+            };
+            run(std::integral_constant<int, 0>{});
+            run(std::integral_constant<int, 1>{});
+            run(std::integral_constant<int, 2>{});
+            run(std::integral_constant<int, 3>{});
         }
-        for (int xs = imax(0, W - L); xs < W; xs++) emit(xs);
         __syncwarp();
     }
 }
 
 // ---------------------------------------------------------------------------
-// vert: block per (view, column, strip of R output rows).  The strip's rows
-// y0-L .. y0+R+L-1 (segments and geometry words of all disparities) are copied
-// into shared memory with cp.async (all in flight at once); a column-wise
-// running count of the row pixel counts (integers, so exact) replaces the
-// per-row count additions; each warp then owns whole output rows.
-constexpr int kVertT = 256;
+// vert: block per (view, column x, strip of rows).  Rows enter a shared ring 8
+// at a time ("ticks", warp w ingesting row w of the tick); for every entry the
+// ring holds the row segment and the row's pixel count l + r + 1, and the
+// entry's vertical arms t | b << 8.  Each step a warp computes one output row
+// y: it walks the rows of the reference pixel's own vertical arm (a superset of
+// every disparity's arm) and adds a row's segment and count where the row lies
+// in that disparity's arm [y - t, y + b], top to bottom
+// (seq/CrossBasedAggregation.cpp:140-164); the average is the correctly rounded
+// quotient (:166) and the winner the first strict minimum over d.
+constexpr int kVertW = 8;
+constexpr int kVertT = kVertW * 32;
 
-__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
-    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
+// ring depth in rows for arm length L: ticks before the first step plus one
+// (a tick may be written while slower warps still read the previous step)
+static int vert_depth(int L) { return 8 * ((2 * L + 8 + 7) / 8 + 1); }
+
+// sum += s and cnt += n when the predicate holds, as predicated instructions (a
+// branch per row and disparity would cost more than the two adds)
+__device__ __forceinline__ void add_if_nz(uint32_t w, float &sum, uint32_t &cnt, float s, uint32_t n) {
+    asm("{\n\t.reg .pred p;\n\tsetp.ne.u32 p, %2, 0;\n\t@p add.rn.f32 %0, %0, %3;\n\t@p add.u32 %1, %1, %4;\n\t}"
+        : "+f"(sum), "+r"(cnt)
+        : "r"(w), "f"(s), "r"(n));
 }
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+__device__ __forceinline__ void add_if_lt(uint32_t a, uint32_t b, float &sum, uint32_t &cnt, float s, uint32_t n) {
+    asm("{\n\t.reg .pred p;\n\tsetp.lo.u32 p, %2, %3;\n\t@p add.rn.f32 %0, %0, %4;\n\t@p add.u32 %1, %1, %5;\n\t}"
+        : "+f"(sum), "+r"(cnt)
+        : "r"(a), "r"(b), "f"(s), "r"(n));
+}
 
-template <typename ST, int NCH>
-__global__ void __launch_bounds__(kVertT) k_vert_views(ViewTable t, int L, int R) {
-    // NCH: 32-disparity chunks per column (D <= 32 * NCH)
-    extern __shared__ __align__(16) unsigned char vsm[];
-    __shared__ uint32_t armr[256];  // packed arms of the reference pixel (row, x) of the strip
-    const int nv = t.nviews;
-    const int *off = t.off + ST_VERT * (nv + 1);
+template <typename ST> struct VRing;
+template <> struct VRing<float> {
+    using E = uint2;   // {segment bits, row pixel count}
+    using In = float;  // what the ingest loads from the segment volume
+    static __device__ __forceinline__ E make(float s, uint32_t cnt) { return make_uint2(__float_as_uint(s), cnt); }
+    static __device__ __forceinline__ float seg(E e) { return __uint_as_float(e.x); }
+    static __device__ __forceinline__ uint32_t cnt_word(E e) { return e.y; }
+    static __device__ __forceinline__ uint32_t cnt_final(uint32_t a) { return a; }
+};
+template <> struct VRing<__half> {
+    // count in the low half (sums of whole words keep it exact below 2^16),
+    // f16 segment in the high half
+    using E = uint32_t;
+    using In = unsigned short;  // the f16 bits
+    static __device__ __forceinline__ E make(unsigned short s, uint32_t cnt) { return ((uint32_t)s << 16) | cnt; }
+    static __device__ __forceinline__ float seg(E e) {
+        float f;
+        asm("{\n\t.reg .b16 lo, hi;\n\tmov.b32 {lo, hi}, %1;\n\tcvt.f32.f16 %0, hi;\n\t}" : "=f"(f) : "r"(e));
+        return f;
+    }
+    static __device__ __forceinline__ uint32_t cnt_word(E e) { return e; }
+    static __device__ __forceinline__ uint32_t cnt_final(uint32_t a) { return a & 0xffffu; }
+};
+
+// One item (column x, rows y0 .. y1-1) with NC 32-disparity chunks per lane;
+// DM is the ring row stride (entries) of the launch.
+template <typename ST, int NC, int DM, int POS>
+__device__ __forceinline__ void vert_item(const ViewDesc &V, int x, int y0, int y1, int L, int DEP,
+                                          const float *__restrict__ rcp, unsigned char *vsm) {
+    using RG = VRing<ST>;
+    using E = typename RG::E;
+    using In = typename RG::In;
+    E *ring = reinterpret_cast<E *>(vsm);                                                // [DEP][DM]
+    uint16_t *inf = reinterpret_cast<uint16_t *>(vsm + (size_t)DEP * DM * sizeof(E));    // [DEP][DM]
+    uint32_t *rinf = reinterpret_cast<uint32_t *>(inf + (size_t)DEP * DM);               // [DEP]
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (int item = blockIdx.x; item < t.total[ST_VERT]; item += gridDim.x) {
-        const int v = find_view(off, nv, item);
-        const ViewDesc &V = t.views[v];
-        const int W = V.W, H = V.H, D = V.D;
-        const int strips = (H + R - 1) / R;
-        const int local = item - __ldg(off + v);
-        const int x = local / strips, strip = local - x * strips;
-        const int y0 = strip * R, y1 = imin(H, y0 + R);
-        const int ya0 = imax(0, y0 - L), ya1 = imin(H, y1 + L);
-        const int nr = ya1 - ya0;
-        const ST *seg = reinterpret_cast<const ST *>(V.seg);
-        ST *S = reinterpret_cast<ST *>(vsm);
-        uint16_t *G = reinterpret_cast<uint16_t *>(vsm + (size_t)(R + 2 * L) * D * sizeof(ST));
-        // column prefix of the row pixel counts: CP[r*D + d] = sum of counts of rows < r
-        // (at most (R + 2L) * (2L + 1) < 65536)
-        uint16_t *CP = reinterpret_cast<uint16_t *>(vsm + (size_t)(R + 2 * L) * D * (sizeof(ST) + 2));
-        __syncthreads();  // previous item done with the tile
-        {
-            constexpr int SV = 16 / sizeof(ST);
-            const int sv_row = D / SV, g_row = D / 8;
-            const int per_row = sv_row + g_row;
-            for (int q = threadIdx.x; q < nr * per_row; q += kVertT) {
-                const int ri = q / per_row, k = q - ri * per_row;
-                const size_t src = ((size_t)(ya0 + ri) * W + x) * D;
-                if (k < sv_row) cp_async16(reinterpret_cast<uint4 *>(S + (size_t)ri * D) + k,
-                                           reinterpret_cast<const uint4 *>(seg + src) + k);
-                else cp_async16(reinterpret_cast<uint4 *>(G + (size_t)ri * D) + (k - sv_row),
-                                reinterpret_cast<const uint4 *>(V.geo + src) + (k - sv_row));
-            }
-            for (int ri = threadIdx.x; ri < nr; ri += kVertT) armr[ri] = V.rref[(size_t)(ya0 + ri) * W + x].w;
-            cp_async_wait_all();
-        }
-        __syncthreads();
-        for (int d = threadIdx.x; d < D; d += kVertT) {
-            int acc = 0;
-            for (int ri = 0; ri < nr; ri++) {
-                CP[ri * D + d] = (uint16_t)acc;
-                acc += G[ri * D + d] & 63;
-            }
-            CP[nr * D + d] = (uint16_t)acc;
-        }
-        __syncthreads();
-        for (int yo = y0 + warp; yo < y1; yo += kVertT / 32) {
-            const int ro = yo - ya0;
-            // every disparity's vertical arm is inside the reference pixel's own arm
-            const uint32_t ar = armr[ro];
-            const int rlo = ro - (int)((ar >> 16) & 0xff), rhi = ro + (int)(ar >> 24);
-            const int nch = (D + 31) >> 5;  // this view's chunks (<= NCH)
-            int lo[NCH];
-            unsigned span[NCH];
-            float sum[NCH];
+    const int W = V.W, H = V.H, D = V.D, mir = V.mirror;
+    const int ra = imax(0, y0 - L), rb = imin(H, y1 + L);
+    const int xsrc = mir ? W - 1 - x : x;
+    // per chunk: this lane's disparity, whether it exists, its target image column
+    int tcol[NC];
+    bool dok[NC];
 #pragma unroll
-            for (int c = 0; c < NCH; c++) {
-                const int d = c * 32 + lane;
-                const int g = (c < nch && d < D) ? G[ro * D + d] : 0;
-                lo[c] = ro - ((g >> 6) & 31);
-                // rows lo .. lo+span; lanes past D get an empty range
-                span[c] = (c < nch && d < D) ? (unsigned)((g >> 11) + ((g >> 6) & 31)) : 0xffffffffu;
+    for (int c = 0; c < NC; c++) {
+        const int d = 32 * c + lane;
+        dok[c] = d < D;
+        int xt = x - (dok[c] ? d : 0);
+        if (xt < 0) xt += W;  // seq/PixelBasedCost.cpp:19-20 (D <= W)
+        tcol[c] = mir ? W - 1 - xt : xt;
+    }
+    const In *segx = reinterpret_cast<const In *>(V.seg) + (size_t)x * D + lane;  // + r W D + 32 c
+    const size_t segrow = (size_t)W * D;
+    const int nticks = (rb - ra + 7) >> 3;
+    // one tick's loads for this warp's row, in flight while the previous tick is used
+    In pseg[NC];
+    uint2 ptar[NC], pref;
+    auto load_tick = [&](int i) {
+        const int r = ra + 8 * i + warp;
+        if (r < rb) {
+            const uint2 *arow = V.atar + (size_t)r * W;
+            pref = V.aref[(size_t)r * W + xsrc];
+#pragma unroll
+            for (int c = 0; c < NC; c++) {
+                if (dok[c]) pseg[c] = segx[(size_t)r * segrow + 32 * c];
+                ptar[c] = arow[tcol[c]];
+            }
+        }
+    };
+    int tslot = 0;  // ring slot of the next tick's first row
+    // tick i into the ring, then the loads of tick i + 1 (used by the next step)
+    auto ingest = [&](int i) {
+        const int r = ra + 8 * i + warp;
+        if (r < rb) {
+            const int slot = tslot + warp;
+            E *er = ring + slot * DM + lane;
+            uint16_t *ir = inf + slot * DM + lane;
+#pragma unroll
+            for (int c = 0; c < NC; c++) {
+                const uint32_t m = __vminu2(pref.x, ptar[c].x);   // l | r << 16
+                const uint32_t cnt = __dp2a_lo(m, 0x0101u, 1u);   // l + r + 1
+                const uint32_t tb = __vminu2(pref.y, ptar[c].y);  // t | b << 16
+                // t | (t + b + 1) << 8: the start and length of the arm; 0 for no disparity
+                const uint32_t tw = __dp2a_lo(tb, 0x0101u, 1u) << 8 | (tb & 0xffu);
+                if (dok[c]) er[32 * c] = RG::make(pseg[c], cnt);
+                ir[32 * c] = dok[c] ? (uint16_t)tw : (uint16_t)0;
+            }
+            if (lane == 0) rinf[slot] = __byte_perm(pref.y, 0, 0x4420);
+        }
+        tslot += 8;
+        if (tslot == DEP) tslot = 0;
+        if (i + 1 < nticks) load_tick(i + 1);
+    };
+    __syncthreads();  // the previous item's readers are done with the ring
+    load_tick(0);
+    const int T0 = (y0 + 8 + L - ra + 7) >> 3;  // ticks the first step needs
+    int i = 0;
+    for (; i < T0 - 1; i++) ingest(i);
+    const int nsteps = (y1 - y0 + 7) >> 3;
+    int sbase = y0 - ra;  // ring slot of row y0 + 8s (< DEP)
+    for (int s = 0; s < nsteps; s++, i++) {
+        ingest(i);
+        __syncthreads();
+        const int y = y0 + 8 * s + warp;
+        if (y < y1) {
+            int sy = sbase + warp;
+            if (sy >= DEP) sy -= DEP;
+            const uint32_t ri = rinf[sy];
+            const int tr = ri & 0xff, br = ri >> 8;
+            const int K = tr + br + 1;
+            int slot = sy - tr;
+            if (slot < 0) slot += DEP;
+            int lo[NC], len[NC];
+            float sum[NC];
+            uint32_t cacc[NC];
+#pragma unroll
+            for (int c = 0; c < NC; c++) {
+                const uint32_t info = inf[sy * DM + 32 * c + lane];
+                lo[c] = tr - (int)(info & 0xff);  // row y - t, counted from y - tr
+                len[c] = (int)(info >> 8);        // t + b + 1 rows (0: no disparity)
                 sum[c] = 0.f;
+                cacc[c] = 0;
             }
-            // seq/CrossBasedAggregation.cpp:146-164: row segments of each (x, d) top to
-            // bottom; a row outside that disparity's own arm is skipped, not added
-            for (int r = rlo; r <= rhi; r++) {
+            // rows y - tr .. y + br, top to bottom, wrapping once in the ring
+            if (K <= 32) {
+                uint32_t msk[NC];
 #pragma unroll
-                for (int c = 0; c < NCH; c++) {
-                    if (c < nch && (unsigned)(r - lo[c]) <= span[c])
-                        sum[c] = __fadd_rn(sum[c], to_f32(S[r * D + c * 32 + lane]));
+                for (int c = 0; c < NC; c++)
+                    asm("bmsk.clamp.b32 %0, %1, %2;" : "=r"(msk[c]) : "r"(lo[c]), "r"(len[c]));
+                uint32_t bit = 1;
+                for (int k = 0; k < K; k++) {
+                    const E *rp = ring + slot * DM + lane;
+#pragma unroll
+                    for (int c = 0; c < NC; c++) {
+                        const E e = rp[32 * c];
+                        add_if_nz(msk[c] & bit, sum[c], cacc[c], RG::seg(e), RG::cnt_word(e));
+                    }
+                    bit <<= 1;
+                    if (++slot == DEP) slot = 0;
+                }
+            } else {
+                for (int k = 0; k < K; k++) {
+                    const E *rp = ring + slot * DM + lane;
+#pragma unroll
+                    for (int c = 0; c < NC; c++) {
+                        const E e = rp[32 * c];
+                        // k in [lo, lo + len): k - lo < len as unsigned
+                        add_if_lt((uint32_t)(k - lo[c]), (uint32_t)len[c], sum[c], cacc[c], RG::seg(e),
+                                  RG::cnt_word(e));
+                    }
+                    if (++slot == DEP) slot = 0;
                 }
             }
             uint32_t best_key = 0xffffffffu;
             int best_d = 0;
 #pragma unroll
-            for (int c = 0; c < NCH; c++) {
-                if (c >= nch) break;
-                const int d = c * 32 + lane;
-                uint32_t key = 0xffffffffu;
-                if (d < D) {
-                    const int cnt = CP[(lo[c] + (int)span[c] + 1) * D + d] - CP[lo[c] * D + d];
-                    key = order_key(__fdiv_rn(sum[c], (float)cnt));  // :166
-                }
-                const uint32_t m = __reduce_min_sync(0xffffffffu, key);
-                if (m < best_key) {  // strict: an earlier chunk keeps ties
-                    const unsigned hit = __ballot_sync(0xffffffffu, key == m);
-                    best_key = m;
-                    best_d = c * 32 + __ffs(hit) - 1;
+            for (int c = 0; c < NC; c++) {
+                if (dok[c]) {
+                    const uint32_t cnt = RG::cnt_final(cacc[c]);
+                    uint32_t key;
+                    if constexpr (POS) {
+                        // sums of non-negative costs: the correctly rounded quotient by
+                        // Markstein's correction from a correctly rounded reciprocal
+                        // (Markstein 1990; exact residual by FMA), and the bits of a
+                        // non-negative float order like the float
+                        const float rcb = __ldg(rcp + cnt);
+                        const float q0 = __fmul_rn(sum[c], rcb);
+                        const float rr = __fmaf_rn(-(float)cnt, q0, sum[c]);
+                        key = __float_as_uint(__fmaf_rn(rr, rcb, q0));
+                    } else {
+                        key = order_key(__fdiv_rn(sum[c], (float)cnt));
+                    }
+                    if (key < best_key) {  // strict: the lowest d keeps ties
+                        best_key = key;
+                        best_d = 32 * c + lane;
+                    }
                 }
             }
+            const uint32_t m = __reduce_min_sync(0xffffffffu, best_key);
+            const uint32_t bd = __reduce_min_sync(0xffffffffu, best_key == m ? (uint32_t)best_d : 0xffffu);
             if (lane == 0) {
-                const bool found = best_d != 0;  // some d >= 1 strictly below cost[0]
-                V.raw[(size_t)yo * W + x] = found ? (uint16_t)(0x100 | best_d) : (uint16_t)0;
-                if (found) atomicMax(V.row_last + yo, x);
+                const bool found = bd != 0;  // some d >= 1 strictly below cost[0]
+                V.raw[(size_t)y * W + x] = found ? (uint16_t)(0x100 | bd) : (uint16_t)0;
+                if (found) atomicMax(V.row_last + y, x);
             }
         }
+        sbase += 8;
+        if (sbase >= DEP) sbase -= DEP;
+    }
+}
+
+template <typename ST, int NCH, int POS>
+__global__ void __launch_bounds__(kVertT, NCH <= 4 ? 3 : 1)
+    k_vert_views(ViewTable t, int L, int R, int DEP, const float *__restrict__ rcp) {
+    constexpr int DM = 32 * NCH;  // ring row stride in entries
+    extern __shared__ __align__(16) unsigned char vsm[];
+    const int nv = t.nviews;
+    const int *off = t.off + ST_VERT * (nv + 1);
+    for (int item = blockIdx.x; item < t.total[ST_VERT]; item += gridDim.x) {
+        const int v = find_view(off, nv, item);
+        const ViewDesc &V = t.views[v];
+        const int H = V.H;
+        const int strips = (H + R - 1) / R;
+        const int local = item - __ldg(off + v);
+        const int x = local / strips, strip = local - x * strips;
+        const int y0 = strip * R, y1 = imin(H, y0 + R);
+        const int nch = (V.D + 31) >> 5;
+        if (nch <= 1 || NCH == 1) vert_item<ST, 1, DM, POS>(V, x, y0, y1, L, DEP, rcp, vsm);
+        else if (nch <= 2 || NCH == 2) vert_item<ST, (NCH >= 2 ? 2 : 1), DM, POS>(V, x, y0, y1, L, DEP, rcp, vsm);
+        else if (nch <= 4 || NCH == 4) vert_item<ST, (NCH >= 4 ? 4 : 1), DM, POS>(V, x, y0, y1, L, DEP, rcp, vsm);
+        else vert_item<ST, NCH, DM, POS>(V, x, y0, y1, L, DEP, rcp, vsm);
     }
 }
 
@@ -432,13 +595,13 @@ __global__ void __launch_bounds__(256) k_cc_views(ViewTable t) {
 }
 
 // ---------------------------------------------------------------------------
-int stage_items(int stage, int W, int H, int D, int vert_rows) {
+int stage_items(int stage, const ViewDesc &v, int vert_rows) {
     switch (stage) {
-    case ST_PREP: return 2 * H * ((W + kPrepSeg - 1) / kPrepSeg);
-    case ST_HSEG: return H * ((D + 31) / 32);
-    case ST_VERT: return W * ((H + vert_rows - 1) / vert_rows);
-    case ST_FILL: return H;
-    case ST_CC: return H;
+    case ST_PREP: return v.prep ? 2 * ((v.W + kPrepTW - 1) / kPrepTW) * ((v.H + kPrepTH - 1) / kPrepTH) : 0;
+    case ST_HSEG: return v.H * ((v.D + 31) / 32);
+    case ST_VERT: return v.W * ((v.H + vert_rows - 1) / vert_rows);
+    case ST_FILL: return v.H;
+    case ST_CC: return v.H;
     }
     return 0;
 }
@@ -454,8 +617,31 @@ static int num_sms() {
     return n;
 }
 
-rts_status launch_cross_views(rts_ctx *c, const rts_params &p, const ViewTable &t, int half, int has_vol, int max_d,
-                              const CrossTune &tune, int *row_last_all, size_t row_last_count) {
+template <typename K> static int resident_blocks(K kern, int threads, size_t smem) {
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kern, threads, smem) != cudaSuccess || n < 1) n = 1;
+    return n;
+}
+
+static bool mode1(const rts_params &p) {
+    // AD (truncated, seq/Main.cpp:183-186) + census with an integral truncation
+    return p.cost1 == RTS_COST_AD && p.cost2 == RTS_COST_CENSUS && p.ad_trunc >= 0.f &&
+           p.ad_trunc < (float)kCombineLut && p.ad_trunc == floorf(p.ad_trunc);
+}
+
+rts_status cross_tables(rts_ctx *c, const rts_params &p) {
+    const float *t;
+    if (mode1(p)) RTS_TRY(combine_lut2d(c, p.lambda1, p.lambda2, (int)p.ad_trunc, &t));
+    else if (p.cost2 != RTS_COST_NONE) {
+        const float *t2;
+        RTS_TRY(combine_luts(c, p.lambda1, p.lambda2, &t, &t2));
+    }
+    RTS_TRY(recip_table(c, &t));
+    return RTS_OK;
+}
+
+rts_status launch_cross_views(rts_ctx *c, const rts_params &p, const ViewTable &t, int half, int has_vol, int gray,
+                              int max_d, const CrossTune &tune, int *row_last_all, size_t row_last_count) {
     CostCfg cfg;
     cfg.k1 = p.cost1;
     cfg.k2 = p.cost2;
@@ -470,7 +656,12 @@ rts_status launch_cross_views(rts_ctx *c, const rts_params &p, const ViewTable &
                                          p.ad_trunc == floorf(p.ad_trunc));
     cfg.int_path = trunc_ok ? 1 : 0;
     cfg.itrunc = cfg.trunc1 ? (int)p.ad_trunc : 0x7fffffff;
-    if (p.cost2 != RTS_COST_NONE) RTS_TRY(combine_luts(c, p.lambda1, p.lambda2, &cfg.lut1, &cfg.lut2));
+    const int mode = has_vol ? 0 : mode1(p) ? 1 : 2;
+    const float *lut2d = nullptr, *rcp = nullptr;
+    if (mode == 1) RTS_TRY(combine_lut2d(c, p.lambda1, p.lambda2, (int)p.ad_trunc, &lut2d));
+    else if (p.cost2 != RTS_COST_NONE) RTS_TRY(combine_luts(c, p.lambda1, p.lambda2, &cfg.lut1, &cfg.lut2));
+    RTS_TRY(recip_table(c, &rcp));
+    const int grayrec = (mode == 1 && gray) ? 1 : 0;
     cudaStream_t s = c->stream;
     const int sms = num_sms();
     auto grid = [&](int items, int per_block, int per_sm) {
@@ -478,57 +669,70 @@ rts_status launch_cross_views(rts_ctx *c, const rts_params &p, const ViewTable &
         const long cap = (long)sms * per_sm;
         return (unsigned)(need < cap ? (need > 0 ? need : 1) : cap);
     };
-    const int L = p.cross_arm, R = tune.vert_rows;
+    const int L = p.cross_arm;
     RTS_CU(c, cudaMemsetAsync(row_last_all, 0xff, row_last_count * sizeof(int), s));
     const bool want_code = !has_vol && (p.cost1 == RTS_COST_CENSUS || p.cost2 == RTS_COST_CENSUS);
-    {
+    if (t.total[ST_PREP] > 0) {
         StageScope sc(c, "prep");
-        const int hr = p.census_hrad, wr = p.census_wrad;
-        const size_t smem = (((2 * hr + 1) * (kPrepSeg + 2 * wr) + 15) & ~15) + 4 * (kPrepSeg + 2 * L) +
-                            4 * (size_t)(2 * L + 1) * kPrepSeg;
-        cudaFuncSetAttribute(k_prep_views, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k_prep_views<<<grid(t.total[ST_PREP], 1, 16), kPrepSeg, smem, s>>>(t, hr, wr, L, p.cross_tau,
-                                                                          want_code ? 1 : 0);
+        const int hr = want_code ? p.census_hrad : 0, wr = want_code ? p.census_wrad : 0;
+        const size_t smem = prep_smem(hr, wr, L);
+        auto go = [&](auto kern) {
+            cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            kern<<<grid(t.total[ST_PREP], 1, resident_blocks(kern, kPrepT, smem)), kPrepT, smem, s>>>(
+                t, hr, wr, L, p.cross_tau, want_code ? 1 : 0);
+        };
+        if (grayrec) go(k_prep_views<1>);
+        else go(k_prep_views<0>);
         count_launch(c);
     }
     {
         StageScope sc(c, "cross_hseg");
-        const unsigned g = grid(t.total[ST_HSEG], kHsegW, 8 * tune.grid_mult);
-        const int mode = has_vol ? 0
-                         : (cfg.int_path && cfg.k1 == RTS_COST_AD && cfg.trunc1 && cfg.k2 == RTS_COST_CENSUS) ? 1
-                                                                                                               : 2;
-        auto go = [&](auto kern) { kern<<<g, kHsegW * 32, 0, s>>>(t, cfg, L); };
+        const unsigned g = grid(t.total[ST_HSEG], kHsegW, tune.grid_mult);
+        auto go = [&](auto kern) { kern<<<g, kHsegW * 32, 0, s>>>(t, cfg, lut2d); };
         if (half) {
-            if (mode == 0) go(k_hseg_views<__half, 0>);
-            else if (mode == 1) go(k_hseg_views<__half, 1>);
-            else go(k_hseg_views<__half, 2>);
+            if (mode == 0) go(k_hseg_views<__half, 0, 0>);
+            else if (mode == 1 && grayrec) go(k_hseg_views<__half, 1, 1>);
+            else if (mode == 1) go(k_hseg_views<__half, 1, 0>);
+            else go(k_hseg_views<__half, 2, 0>);
         } else {
-            if (mode == 0) go(k_hseg_views<float, 0>);
-            else if (mode == 1) go(k_hseg_views<float, 1>);
-            else go(k_hseg_views<float, 2>);
+            if (mode == 0) go(k_hseg_views<float, 0, 0>);
+            else if (mode == 1 && grayrec) go(k_hseg_views<float, 1, 1>);
+            else if (mode == 1) go(k_hseg_views<float, 1, 0>);
+            else go(k_hseg_views<float, 2, 0>);
         }
         count_launch(c);
     }
     {
         StageScope sc(c, "cross_vert_wta");
-        const size_t smem = (size_t)(R + 2 * L) * max_d * ((half ? 2 : 4) + 2) + (size_t)(R + 2 * L + 1) * max_d * 2;
-        const unsigned g = grid(t.total[ST_VERT], 1, 2 * tune.grid_mult);
+        const int DEP = vert_depth(L);
+        const int nch = (max_d + 31) / 32;
+        const int NCH = nch <= 1 ? 1 : nch <= 2 ? 2 : nch <= 4 ? 4 : 8;
+        const size_t esz = half ? 4 : 8;
+        const size_t smem = (size_t)DEP * 32 * NCH * (esz + 2) + (size_t)DEP * 4;
+        const int R = tune.vert_rows;
         auto go = [&](auto kern) {
             cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            kern<<<g, kVertT, smem, s>>>(t, L, R);
+            kern<<<grid(t.total[ST_VERT], 1, resident_blocks(kern, kVertT, smem)), kVertT, smem, s>>>(t, L, R, DEP,
+                                                                                                   rcp);
         };
-        const int nch = (max_d + 31) / 32;
+        // non-negative costs (every cost computed from records) take the fast exact division
+#define RTS_VERT(ST, N)                                   \
+    do {                                                  \
+        if (mode == 0) go(k_vert_views<ST, N, 0>);        \
+        else go(k_vert_views<ST, N, 1>);                  \
+    } while (0)
         if (half) {
-            if (nch <= 1) go(k_vert_views<__half, 1>);
-            else if (nch <= 2) go(k_vert_views<__half, 2>);
-            else if (nch <= 4) go(k_vert_views<__half, 4>);
-            else go(k_vert_views<__half, 8>);
+            if (NCH == 1) RTS_VERT(__half, 1);
+            else if (NCH == 2) RTS_VERT(__half, 2);
+            else if (NCH == 4) RTS_VERT(__half, 4);
+            else RTS_VERT(__half, 8);
         } else {
-            if (nch <= 1) go(k_vert_views<float, 1>);
-            else if (nch <= 2) go(k_vert_views<float, 2>);
-            else if (nch <= 4) go(k_vert_views<float, 4>);
-            else go(k_vert_views<float, 8>);
+            if (NCH == 1) RTS_VERT(float, 1);
+            else if (NCH == 2) RTS_VERT(float, 2);
+            else if (NCH == 4) RTS_VERT(float, 4);
+            else RTS_VERT(float, 8);
         }
+#undef RTS_VERT
         count_launch(c);
     }
     {

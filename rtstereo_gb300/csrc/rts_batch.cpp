@@ -92,7 +92,7 @@ void fill_views(ViewBatch &b, int n, const rts_pair *pairs, const rts_out *outs,
             r.disp = outs[i].disp_right;
             r.vol = nullptr;
             l.mask = outs[i].mask;
-            l.partner = 2 * i + 1;
+            link_pair(&b, 2 * i, 2 * i + 1);
         }
     }
 }
@@ -113,7 +113,8 @@ void view_dims(int n, const rts_pair *pairs, const rts_params *params, int right
 }
 
 // Candidate tiles of the autotuner.
-const CrossTune kTuneCandidates[] = {{32, 2}, {64, 2}, {128, 2}, {32, 4}, {64, 4}, {128, 4}, {64, 8}};
+// (strip rows of the vertical kernel, row-segment blocks per SM)
+const CrossTune kTuneCandidates[] = {{4096, 8}, {256, 8}, {96, 8}, {4096, 6}};
 
 }  // namespace
 
@@ -166,8 +167,10 @@ rts_status rts::batch_views_run(rts_ctx *c, int n, const rts_pair *pairs, const 
     void *arena;
     RTS_TRY(scratch(c, SL_BATCH0, bytes, &arena));
     // the tables the kernels read must hold this lambda pair before any replay
-    const float *l1, *l2;
-    if (p.cost2 != RTS_COST_NONE) RTS_TRY(combine_luts(c, p.lambda1, p.lambda2, &l1, &l2));
+    RTS_TRY(cross_tables(c, p));
+    int gray = 1;  // records hold the gray byte as colour only when no pair has colour images
+    for (int i = 0; i < n; i++)
+        if (pairs[i].left_rgb && pairs[i].right_rgb) gray = 0;
     ViewBatch b;
     plan_views_at(arena, W.data(), H.data(), D.data(), nv, half, &b);
     fill_views(b, n, pairs, outs, right);
@@ -185,7 +188,7 @@ rts_status rts::batch_views_run(rts_ctx *c, int n, const rts_pair *pairs, const 
             ViewTable t;
             RTS_TRY(upload_views(c, b, cand, nullptr, &t));
             RTS_CU(c, cudaEventRecord(e0, c->stream));
-            RTS_TRY(launch_cross_views(c, p, t, half, 0, b.max_d, cand, b.row_last_all, b.row_last_count));
+            RTS_TRY(launch_cross_views(c, p, t, half, 0, gray, b.max_d, cand, b.row_last_all, b.row_last_count));
             RTS_CU(c, cudaEventRecord(e1, c->stream));
             RTS_CU(c, cudaEventSynchronize(e1));
             float ms = 0;
@@ -206,7 +209,7 @@ rts_status rts::batch_views_run(rts_ctx *c, int n, const rts_pair *pairs, const 
     RTS_TRY(upload_views(c, b, tune, nullptr, &t));
     if (c->timing) {
         // stage timing wants an event pair around every kernel: launch directly
-        return launch_cross_views(c, p, t, half, 0, b.max_d, tune, b.row_last_all, b.row_last_count);
+        return launch_cross_views(c, p, t, half, 0, gray, b.max_d, tune, b.row_last_all, b.row_last_count);
     }
     GraphEntry &g = gc->graphs[key];
     if (g.exec && (g.arena != arena || g.arena_bytes != bytes)) {
@@ -221,7 +224,7 @@ rts_status rts::batch_views_run(rts_ctx *c, int n, const rts_pair *pairs, const 
         const uint64_t l0 = c->launches.load();
         cudaGraph_t graph;
         RTS_CU(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-        rts_status st = launch_cross_views(c, p, t, half, 0, b.max_d, tune, b.row_last_all, b.row_last_count);
+        rts_status st = launch_cross_views(c, p, t, half, 0, gray, b.max_d, tune, b.row_last_all, b.row_last_count);
         cudaError_t ce = cudaStreamEndCapture(c->stream, &graph);
         c->timing = timing;
         if (st != RTS_OK) return st;
@@ -417,6 +420,9 @@ rts_status launch_batch(rts_server *s, std::vector<Request *> &ids) {
     std::vector<int> W, H, D;
     view_dims(n, pairs.data(), params.data(), right, W, H, D);
     const int nv = right ? 2 * n : n;
+    int gray = 1;
+    for (int i = 0; i < n; i++)
+        if (pairs[i].left_rgb && pairs[i].right_rgb) gray = 0;
     bt.arena_bytes = views_bytes(W.data(), H.data(), D.data(), nv, half);
     bt.arena = s->pool.alloc(bt.arena_bytes);
     if (!bt.arena) return RTS_ERR_BUSY;
@@ -435,7 +441,7 @@ rts_status launch_batch(rts_server *s, std::vector<Request *> &ids) {
         ViewTable t;
         CrossTune tune;
         st = upload_views(c, b, tune, nullptr, &t);
-        if (st == RTS_OK) st = launch_cross_views(c, p, t, half, 0, b.max_d, tune, b.row_last_all, b.row_last_count);
+        if (st == RTS_OK) st = launch_cross_views(c, p, t, half, 0, gray, b.max_d, tune, b.row_last_all, b.row_last_count);
     }
     for (int i = 0; i < n && st == RTS_OK; i++) {
         Request &r = *ids[i];

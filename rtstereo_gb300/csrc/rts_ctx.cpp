@@ -189,6 +189,44 @@ rts_status combine_luts(rts_ctx *c, float lambda1, float lambda2, const float **
     return RTS_OK;
 }
 
+rts_status combine_lut2d(rts_ctx *c, float lambda1, float lambda2, int trunc, const float **t) {
+    const size_t n = (size_t)(trunc + 1) * 65;
+    void *d;
+    RTS_TRY(scratch(c, SL_LUT2D, n * sizeof(float), &d));
+    if (c->lut2d_key.a != lambda1 || c->lut2d_key.b != lambda2 || c->lut2d_key.n != trunc) {
+        std::vector<float> tab(n);
+        for (int s = 0; s <= trunc; s++) {
+            const float t1 = 1 - expf(-(float)s / lambda1);  // seq/CombineCost.cpp:21-22
+            for (int h = 0; h <= 64; h++) {
+                const float t2 = 1 - expf(-(float)h / lambda2);
+                tab[(size_t)s * 65 + h] = t1 + t2;  // :23
+            }
+        }
+        RTS_CU(c, cudaMemcpyAsync(d, tab.data(), n * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+        RTS_CU(c, cudaStreamSynchronize(c->stream));
+        c->lut2d_key.a = lambda1;
+        c->lut2d_key.b = lambda2;
+        c->lut2d_key.n = trunc;
+    }
+    *t = (const float *)d;
+    return RTS_OK;
+}
+
+rts_status recip_table(rts_ctx *c, const float **r) {
+    void *d;
+    RTS_TRY(scratch(c, SL_RCP, (kRecipMax + 1) * sizeof(float), &d));
+    if (!c->rcp_ready) {
+        std::vector<float> tab(kRecipMax + 1);
+        tab[0] = 0.f;
+        for (int i = 1; i <= kRecipMax; i++) tab[i] = 1.0f / (float)i;
+        RTS_CU(c, cudaMemcpyAsync(d, tab.data(), tab.size() * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+        RTS_CU(c, cudaStreamSynchronize(c->stream));
+        c->rcp_ready = true;
+    }
+    *r = (const float *)d;
+    return RTS_OK;
+}
+
 rts_status lab_weight_lut(rts_ctx *c, float gamma_s, const float **g) {
     void *d;
     size_t n = (size_t)kLabDist2Max + 1;

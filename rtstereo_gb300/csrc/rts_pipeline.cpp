@@ -281,7 +281,7 @@ static rts_status pipeline_cross_views(rts_ctx *c, const rts_params &p, int H, i
         ViewDesc &v1 = b.views[1];
         v1.gref = rg; v1.gtar = lg; v1.cref = rc; v1.ctar = lc; v1.mirror = 1; v1.disp = dr;
         v0.mask = mask;
-        v0.partner = 1;
+        link_pair(&b, 0, 1);
     }
     int has_vol = 0;
     if (!fast_costs(p)) {
@@ -312,8 +312,10 @@ static rts_status pipeline_cross_views(rts_ctx *c, const rts_params &p, int H, i
         }
     }
     ViewTable t;
+    RTS_TRY(cross_tables(c, p));
     RTS_TRY(upload_views(c, b, tune, nullptr, &t));
-    return launch_cross_views(c, p, t, half, has_vol, b.max_d, tune, b.row_last_all, b.row_last_count);
+    return launch_cross_views(c, p, t, half, has_vol, (!lc || !rc) ? 1 : 0, b.max_d, tune, b.row_last_all,
+                              b.row_last_count);
 }
 
 // Prepares device inputs for both views and runs them; all pointers device.
@@ -322,6 +324,10 @@ rts_status pipeline_device(rts_ctx *c, const rts_params &p, int H, int W, const 
                            uint8_t *dr, uint8_t *mask, float *cost_out) {
     const size_t np = (size_t)H * W;
     cudaStream_t s = c->stream;
+    // the cross-based view kernels read gray images directly when there is no colour
+    if (!cost_out && p.aggr == RTS_AGGR_CROSS && cross_fused_supported(p) && fast_costs(p))
+        return pipeline_cross_views(c, p, H, W, lg, rg, lc && rc ? lc : nullptr, lc && rc ? rc : nullptr, dl, dr,
+                                    mask);
     const bool need_lab = p.aggr == RTS_AGGR_AW;
     // the fused kernels read packed colour records even for gray-only costs
     const bool need_rgb = true;

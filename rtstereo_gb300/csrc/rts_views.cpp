@@ -11,7 +11,7 @@ size_t views_bytes(const int *W, const int *H, const int *D, int n, int half) {
     size_t bytes = 0, rl = 0;
     for (int i = 0; i < n; i++) {
         const size_t np = (size_t)W[i] * H[i], ne = np * D[i];
-        bytes += align256(np * 32) + align256(ne * (half ? 2 : 4)) + align256(ne * 2) + align256(np * 2);
+        bytes += align256(np * 32) + align256(np * 16) + align256(ne * (half ? 2 : 4)) + align256(np * 2);
         rl += H[i];
     }
     bytes += align256(rl * 4);
@@ -33,13 +33,15 @@ void plan_views_at(void *arena, const int *W, const int *H, const int *D, int n,
         v.H = H[i];
         v.D = D[i];
         v.partner = -1;
+        v.prep = 1;
         v.rref = (uint4 *)(a + pos);
         v.rtar = v.rref + np;
         pos += align256(np * 32);
+        v.aref = (uint2 *)(a + pos);
+        v.atar = v.aref + np;
+        pos += align256(np * 16);
         v.seg = a + pos;
         pos += align256(ne * (half ? 2 : 4));
-        v.geo = (uint16_t *)(a + pos);
-        pos += align256(ne * 2);
         v.raw = (uint16_t *)(a + pos);
         pos += align256(np * 2);
         rl += H[i];
@@ -54,6 +56,17 @@ void plan_views_at(void *arena, const int *W, const int *H, const int *D, int n,
     }
     pos += align256(rl * 4);
     b->table = a + pos;
+}
+
+void link_pair(ViewBatch *b, int left, int right) {
+    ViewDesc &l = b->views[left], &r = b->views[right];
+    l.prep = 1;
+    l.partner = right;
+    r.prep = 0;
+    r.rref = l.rtar;
+    r.rtar = l.rref;
+    r.aref = l.atar;
+    r.atar = l.aref;
 }
 
 rts_status plan_views(rts_ctx *c, int slot, const int *W, const int *H, const int *D, int n, int half,
@@ -74,7 +87,7 @@ rts_status upload_views(rts_ctx *c, const ViewBatch &bc, const CrossTune &tune, 
         o[0] = 0;
         for (int i = 0; i < n; i++) {
             const ViewDesc &v = b.views[i];
-            int items = stage_items(s, v.W, v.H, v.D, tune.vert_rows);
+            int items = stage_items(s, v, tune.vert_rows);
             if (s == ST_CC && (v.partner < 0 || !v.mask)) items = 0;
             o[i + 1] = o[i] + items;
         }

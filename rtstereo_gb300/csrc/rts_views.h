@@ -3,7 +3,9 @@
 // A view is one direction of one stereo pair: the left view matches the left
 // image against the right one; the right view is the same computation on the
 // horizontally mirrored images (right image as reference), which the kernels
-// read through mirrored addressing instead of flipped copies.  Every stage
+// read through mirrored addressing instead of flipped copies.  The per-pixel
+// records of an image are made once, in image coordinates, by the view that
+// owns them (prep = 1) and shared with the pair's other view.  Every stage
 // kernel runs over all views of a batch in one launch: work items of all views
 // are numbered consecutively and a kernel finds an item's view by binary
 // search in the per-view prefix offsets.
@@ -23,15 +25,15 @@ struct ViewDesc {
     const float *vol;            // optional precomputed cost volume of the view [H][W][D] (or nullptr)
     int mirror;                  // 1: the view reads its sources mirrored in x
     int W, H, D;
-    uint4 *rref, *rtar;          // per-pixel records in view coordinates
-    void *seg;                   // row segments [H][W][D], float or __half
-    uint16_t *geo;               // geometry words [H][W][D]
+    uint4 *rref, *rtar;          // per-pixel records {census lo, census hi, colour, l | r<<16}, image coordinates
+    uint2 *aref, *atar;          // per-pixel arm words {l | r<<16, t | b<<16}, image coordinates
+    void *seg;                   // row segments [H][W][D] in view coordinates, float or __half
     uint16_t *raw;               // winner | found << 8 per pixel
     int *row_last;               // per row: last x with a winner of its own, -1 if none
     uint8_t *disp;               // output disparity (written mirrored back when mirror)
     uint8_t *mask;               // cross-check mask of the pair (left views only), or nullptr
     int partner;                 // index of the right view of the same pair, or -1
-    int pad_;
+    int prep;                    // 1: this view makes the records of both its images
 };
 
 // stage offsets: item k of stage s belongs to view v with off[s][v] <= k < off[s][v+1]
@@ -45,17 +47,22 @@ struct ViewTable {
 };
 
 struct CrossTune {
-    int vert_rows = 64;     // output rows per vertical-aggregation block
-    int grid_mult = 4;      // persistent blocks per SM for the item loops
+    int vert_rows = 4096;   // output rows per vertical-aggregation item (a strip of one column)
+    int grid_mult = 8;      // persistent blocks per SM of the row-segment kernel
 };
 
 // Per-view item counts (host): the layout the kernels and the planner share.
-int stage_items(int stage, int W, int H, int D, int vert_rows);
+int stage_items(int stage, const ViewDesc &v, int vert_rows);
+
+// Host tables the cross-based kernels read (combined cost table, reciprocals);
+// made before a graph capture so that the launches find them cached.
+rts_status cross_tables(rts_ctx *c, const rts_params &p);
 
 // Launches all stages of the cross-based pipeline over a view table that is
-// already on the device; half selects f16 row segments.
-rts_status launch_cross_views(rts_ctx *c, const rts_params &p, const ViewTable &t, int half, int has_vol, int max_d,
-                              const CrossTune &tune, int *row_last_all, size_t row_last_count);
+// already on the device; half selects f16 row segments, gray that no view has
+// an RGB image.
+rts_status launch_cross_views(rts_ctx *c, const rts_params &p, const ViewTable &t, int half, int has_vol, int gray,
+                              int max_d, const CrossTune &tune, int *row_last_all, size_t row_last_count);
 
 // One batch of views on the device, planned on the host.
 struct ViewBatch {
@@ -69,8 +76,8 @@ struct ViewBatch {
 };
 
 // Sizes the scratch of `n` views (W, H, D per view), carves it from the arena
-// slot, fills the device-side buffers of every ViewDesc (records, segments,
-// geometry, winners, row summaries) and the stage offsets.  Image, output and
+// slot, fills the device-side buffers of every ViewDesc (records, arm words,
+// segments, winners, row summaries) and the stage offsets.  Image, output and
 // volume pointers are left for the caller to fill before upload.
 rts_status plan_views(rts_ctx *c, int slot, const int *W, const int *H, const int *D, int n, int half,
                       const CrossTune &tune, ViewBatch *b);
@@ -78,6 +85,9 @@ rts_status plan_views(rts_ctx *c, int slot, const int *W, const int *H, const in
 size_t views_bytes(const int *W, const int *H, const int *D, int n, int half);
 // Carves n views out of an arena of views_bytes() bytes.
 void plan_views_at(void *arena, const int *W, const int *H, const int *D, int n, int half, ViewBatch *b);
+// Makes views `left` and `right` one pair: the left view makes the records of
+// both images, the right view reads them (its reference is the right image).
+void link_pair(ViewBatch *b, int left, int right);
 // Computes the stage offsets, copies the view table and offsets to the device
 // (through the pinned buffer `stage` when given, else directly) and fills `t`.
 rts_status upload_views(rts_ctx *c, const ViewBatch &b, const CrossTune &tune, void *stage, ViewTable *t);
