@@ -309,41 +309,73 @@ constexpr int kVertT = kVertW * 32;
 // (a tick may be written while slower warps still read the previous step)
 static int vert_depth(int L) { return 8 * ((2 * L + 8 + 7) / 8 + 1); }
 
-// sum += s and cnt += n when the predicate holds, as predicated instructions (a
-// branch per row and disparity would cost more than the two adds)
-__device__ __forceinline__ void add_if_nz(uint32_t w, float &sum, uint32_t &cnt, float s, uint32_t n) {
-    asm("{\n\t.reg .pred p;\n\tsetp.ne.u32 p, %2, 0;\n\t@p add.rn.f32 %0, %0, %3;\n\t@p add.u32 %1, %1, %4;\n\t}"
-        : "+f"(sum), "+r"(cnt)
-        : "r"(w), "f"(s), "r"(n));
-}
-__device__ __forceinline__ void add_if_lt(uint32_t a, uint32_t b, float &sum, uint32_t &cnt, float s, uint32_t n) {
-    asm("{\n\t.reg .pred p;\n\tsetp.lo.u32 p, %2, %3;\n\t@p add.rn.f32 %0, %0, %4;\n\t@p add.u32 %1, %1, %5;\n\t}"
-        : "+f"(sum), "+r"(cnt)
-        : "r"(a), "r"(b), "f"(s), "r"(n));
-}
-
+// The ring accumulators: where a row lies in a disparity's arm, its segment is
+// added to the sum and its pixel count to the count, as predicated instructions
+// (a branch per row and disparity would cost more than the two adds).
 template <typename ST> struct VRing;
 template <> struct VRing<float> {
     using E = uint2;   // {segment bits, row pixel count}
     using In = float;  // what the ingest loads from the segment volume
+    struct Acc {
+        float s;
+        uint32_t c;
+    };
     static __device__ __forceinline__ E make(float s, uint32_t cnt) { return make_uint2(__float_as_uint(s), cnt); }
-    static __device__ __forceinline__ float seg(E e) { return __uint_as_float(e.x); }
-    static __device__ __forceinline__ uint32_t cnt_word(E e) { return e.y; }
-    static __device__ __forceinline__ uint32_t cnt_final(uint32_t a) { return a; }
+    static __device__ __forceinline__ Acc zero() { return Acc{0.f, 0u}; }
+    // the entry at shared address a + OFF (bytes)
+    template <int OFF> static __device__ __forceinline__ E lds(uint32_t a) {
+        E e;
+        asm volatile("ld.shared.v2.u32 {%0, %1}, [%2+%3];" : "=r"(e.x), "=r"(e.y) : "r"(a), "n"(OFF));
+        return e;
+    }
+    static __device__ __forceinline__ void add_if_bit(Acc &a, uint32_t m, uint32_t bit, E e) {
+        asm("{\n\t.reg .pred p;\n\t.reg .b32 t;\n\tand.b32 t, %2, %3;\n\tsetp.ne.u32 p, t, 0;\n\t"
+            "@p add.rn.f32 %0, %0, %4;\n\t@p add.u32 %1, %1, %5;\n\t}"
+            : "+f"(a.s), "+r"(a.c)
+            : "r"(m), "r"(bit), "f"(__uint_as_float(e.x)), "r"(e.y));
+    }
+    static __device__ __forceinline__ void add_if_lt(Acc &a, uint32_t x, uint32_t y, E e) {
+        asm("{\n\t.reg .pred p;\n\tsetp.lo.u32 p, %2, %3;\n\t@p add.rn.f32 %0, %0, %4;\n\t@p add.u32 %1, %1, %5;\n\t}"
+            : "+f"(a.s), "+r"(a.c)
+            : "r"(x), "r"(y), "f"(__uint_as_float(e.x)), "r"(e.y));
+    }
+    static __device__ __forceinline__ float sum(Acc a) { return a.s; }
+    static __device__ __forceinline__ uint32_t cnt(Acc a) { return a.c; }
 };
 template <> struct VRing<__half> {
     // count in the low half (sums of whole words keep it exact below 2^16),
     // f16 segment in the high half
     using E = uint32_t;
     using In = unsigned short;  // the f16 bits
+    struct Acc {
+        float s;
+        uint32_t c;
+    };
     static __device__ __forceinline__ E make(unsigned short s, uint32_t cnt) { return ((uint32_t)s << 16) | cnt; }
+    static __device__ __forceinline__ Acc zero() { return Acc{0.f, 0u}; }
+    template <int OFF> static __device__ __forceinline__ E lds(uint32_t a) {
+        E e;
+        asm volatile("ld.shared.u32 %0, [%1+%2];" : "=r"(e) : "r"(a), "n"(OFF));
+        return e;
+    }
     static __device__ __forceinline__ float seg(E e) {
         float f;
         asm("{\n\t.reg .b16 lo, hi;\n\tmov.b32 {lo, hi}, %1;\n\tcvt.f32.f16 %0, hi;\n\t}" : "=f"(f) : "r"(e));
         return f;
     }
-    static __device__ __forceinline__ uint32_t cnt_word(E e) { return e; }
-    static __device__ __forceinline__ uint32_t cnt_final(uint32_t a) { return a & 0xffffu; }
+    static __device__ __forceinline__ void add_if_bit(Acc &a, uint32_t m, uint32_t bit, E e) {
+        asm("{\n\t.reg .pred p;\n\t.reg .b32 t;\n\tand.b32 t, %2, %3;\n\tsetp.ne.u32 p, t, 0;\n\t"
+            "@p add.rn.f32 %0, %0, %4;\n\t@p add.u32 %1, %1, %5;\n\t}"
+            : "+f"(a.s), "+r"(a.c)
+            : "r"(m), "r"(bit), "f"(seg(e)), "r"(e));
+    }
+    static __device__ __forceinline__ void add_if_lt(Acc &a, uint32_t x, uint32_t y, E e) {
+        asm("{\n\t.reg .pred p;\n\tsetp.lo.u32 p, %2, %3;\n\t@p add.rn.f32 %0, %0, %4;\n\t@p add.u32 %1, %1, %5;\n\t}"
+            : "+f"(a.s), "+r"(a.c)
+            : "r"(x), "r"(y), "f"(seg(e)), "r"(e));
+    }
+    static __device__ __forceinline__ float sum(Acc a) { return a.s; }
+    static __device__ __forceinline__ uint32_t cnt(Acc a) { return a.c & 0xffffu; }
 };
 
 // One item (column x, rows y0 .. y1-1) with NC 32-disparity chunks per lane;
@@ -361,17 +393,9 @@ __device__ __forceinline__ void vert_item(const ViewDesc &V, int x, int y0, int 
     const int W = V.W, H = V.H, D = V.D, mir = V.mirror;
     const int ra = imax(0, y0 - L), rb = imin(H, y1 + L);
     const int xsrc = mir ? W - 1 - x : x;
-    // per chunk: this lane's disparity, whether it exists, its target image column
-    int tcol[NC];
-    bool dok[NC];
-#pragma unroll
-    for (int c = 0; c < NC; c++) {
-        const int d = 32 * c + lane;
-        dok[c] = d < D;
-        int xt = x - (dok[c] ? d : 0);
-        if (xt < 0) xt += W;  // seq/PixelBasedCost.cpp:19-20 (D <= W)
-        tcol[c] = mir ? W - 1 - xt : xt;
-    }
+    // per disparity (shared): the target image column of column x
+    int *tcs = reinterpret_cast<int *>(rinf + DEP);  // [DM]
+    auto dok = [&](int c) { return 32 * c + lane < D; };
     const In *segx = reinterpret_cast<const In *>(V.seg) + (size_t)x * D + lane;  // + r W D + 32 c
     const size_t segrow = (size_t)W * D;
     const int nticks = (rb - ra + 7) >> 3;
@@ -385,8 +409,8 @@ __device__ __forceinline__ void vert_item(const ViewDesc &V, int x, int y0, int 
             pref = V.aref[(size_t)r * W + xsrc];
 #pragma unroll
             for (int c = 0; c < NC; c++) {
-                if (dok[c]) pseg[c] = segx[(size_t)r * segrow + 32 * c];
-                ptar[c] = arow[tcol[c]];
+                if (dok(c)) pseg[c] = segx[(size_t)r * segrow + 32 * c];
+                ptar[c] = arow[tcs[32 * c + lane]];
             }
         }
     };
@@ -405,8 +429,8 @@ __device__ __forceinline__ void vert_item(const ViewDesc &V, int x, int y0, int 
                 const uint32_t tb = __vminu2(pref.y, ptar[c].y);  // t | b << 16
                 // t | (t + b + 1) << 8: the start and length of the arm; 0 for no disparity
                 const uint32_t tw = __dp2a_lo(tb, 0x0101u, 1u) << 8 | (tb & 0xffu);
-                if (dok[c]) er[32 * c] = RG::make(pseg[c], cnt);
-                ir[32 * c] = dok[c] ? (uint16_t)tw : (uint16_t)0;
+                if (dok(c)) er[32 * c] = RG::make(pseg[c], cnt);
+                ir[32 * c] = dok(c) ? (uint16_t)tw : (uint16_t)0;
             }
             if (lane == 0) rinf[slot] = __byte_perm(pref.y, 0, 0x4420);
         }
@@ -415,6 +439,12 @@ __device__ __forceinline__ void vert_item(const ViewDesc &V, int x, int y0, int 
         if (i + 1 < nticks) load_tick(i + 1);
     };
     __syncthreads();  // the previous item's readers are done with the ring
+    for (int d = threadIdx.x; d < DM; d += kVertT) {
+        int xt = x - (d < D ? d : 0);
+        if (xt < 0) xt += W;  // seq/PixelBasedCost.cpp:19-20 (D <= W)
+        tcs[d] = mir ? W - 1 - xt : xt;
+    }
+    __syncthreads();
     load_tick(0);
     const int T0 = (y0 + 8 + L - ra + 7) >> 3;  // ticks the first step needs
     int i = 0;
@@ -433,33 +463,53 @@ __device__ __forceinline__ void vert_item(const ViewDesc &V, int x, int y0, int 
             const int K = tr + br + 1;
             int slot = sy - tr;
             if (slot < 0) slot += DEP;
-            int lo[NC], len[NC];
-            float sum[NC];
-            uint32_t cacc[NC];
+            // per disparity: its arm starts at row y - t, counted from y - tr (lo), and has
+            // t + b + 1 rows (len; 0 where there is no disparity)
+            const uint16_t *infy = inf + sy * DM + lane;
+            auto lo = [&](int c) { return tr - (int)(infy[32 * c] & 0xff); };
+            auto len = [&](int c) { return (int)(infy[32 * c] >> 8); };
+            typename RG::Acc acc[NC];
 #pragma unroll
-            for (int c = 0; c < NC; c++) {
-                const uint32_t info = inf[sy * DM + 32 * c + lane];
-                lo[c] = tr - (int)(info & 0xff);  // row y - t, counted from y - tr
-                len[c] = (int)(info >> 8);        // t + b + 1 rows (0: no disparity)
-                sum[c] = 0.f;
-                cacc[c] = 0;
-            }
+            for (int c = 0; c < NC; c++) acc[c] = RG::zero();
             // rows y - tr .. y + br, top to bottom, wrapping once in the ring
-            if (K <= 32) {
+            if (K <= 31) {
+                // blocks of two rows from the even slot at or below the first row (DEP is
+                // even, so a block never straddles the ring's wrap); the bits of the rows of
+                // each disparity's arm, counted from that slot, in msk
+                const int off = slot & 1;
                 uint32_t msk[NC];
 #pragma unroll
                 for (int c = 0; c < NC; c++)
-                    asm("bmsk.clamp.b32 %0, %1, %2;" : "=r"(msk[c]) : "r"(lo[c]), "r"(len[c]));
-                uint32_t bit = 1;
-                for (int k = 0; k < K; k++) {
-                    const E *rp = ring + slot * DM + lane;
-#pragma unroll
-                    for (int c = 0; c < NC; c++) {
-                        const E e = rp[32 * c];
-                        add_if_nz(msk[c] & bit, sum[c], cacc[c], RG::seg(e), RG::cnt_word(e));
+                    asm("bmsk.clamp.b32 %0, %1, %2;" : "=r"(msk[c]) : "r"(lo(c) + off), "r"(len(c)));
+                // 32-bit shared addresses, entries at immediate offsets
+                constexpr int ES = (int)sizeof(E), RS = DM * ES;  // entry, ring row bytes
+                const uint32_t r0 = (uint32_t)__cvta_generic_to_shared(ring + lane);
+                const uint32_t rend = r0 + (uint32_t)(DEP * RS);
+                uint32_t ra = r0 + (uint32_t)((slot - off) * RS);
+                const int nb = (K + off + 1) >> 1;
+                for (int bk = 0; bk < nb; bk++) {
+                    auto chunk = [&](auto cc) {
+                        constexpr int c = decltype(cc)::value;
+                        const E e0 = RG::template lds<32 * c * ES>(ra);
+                        const E e1 = RG::template lds<RS + 32 * c * ES>(ra);
+                        RG::add_if_bit(acc[c], msk[c], 1u, e0);
+                        RG::add_if_bit(acc[c], msk[c], 2u, e1);
+                        msk[c] >>= 2;
+                    };
+                    chunk(std::integral_constant<int, 0>{});
+                    if constexpr (NC > 1) chunk(std::integral_constant<int, 1>{});
+                    if constexpr (NC > 2) {
+                        chunk(std::integral_constant<int, 2>{});
+                        chunk(std::integral_constant<int, 3>{});
                     }
-                    bit <<= 1;
-                    if (++slot == DEP) slot = 0;
+                    if constexpr (NC > 4) {
+                        chunk(std::integral_constant<int, 4>{});
+                        chunk(std::integral_constant<int, 5>{});
+                        chunk(std::integral_constant<int, 6>{});
+                        chunk(std::integral_constant<int, 7>{});
+                    }
+                    ra += 2 * RS;
+                    if (ra == rend) ra = r0;
                 }
             } else {
                 for (int k = 0; k < K; k++) {
@@ -468,8 +518,7 @@ __device__ __forceinline__ void vert_item(const ViewDesc &V, int x, int y0, int 
                     for (int c = 0; c < NC; c++) {
                         const E e = rp[32 * c];
                         // k in [lo, lo + len): k - lo < len as unsigned
-                        add_if_lt((uint32_t)(k - lo[c]), (uint32_t)len[c], sum[c], cacc[c], RG::seg(e),
-                                  RG::cnt_word(e));
+                        RG::add_if_lt(acc[c], (uint32_t)(k - lo(c)), (uint32_t)len(c), e);
                     }
                     if (++slot == DEP) slot = 0;
                 }
@@ -478,20 +527,22 @@ __device__ __forceinline__ void vert_item(const ViewDesc &V, int x, int y0, int 
             int best_d = 0;
 #pragma unroll
             for (int c = 0; c < NC; c++) {
-                if (dok[c]) {
-                    const uint32_t cnt = RG::cnt_final(cacc[c]);
+                if (dok(c)) {
+                    const float sm = RG::sum(acc[c]);
+                    const uint32_t cn = RG::cnt(acc[c]);
+                    const float cf = (float)cn;
                     uint32_t key;
                     if constexpr (POS) {
                         // sums of non-negative costs: the correctly rounded quotient by
                         // Markstein's correction from a correctly rounded reciprocal
                         // (Markstein 1990; exact residual by FMA), and the bits of a
                         // non-negative float order like the float
-                        const float rcb = __ldg(rcp + cnt);
-                        const float q0 = __fmul_rn(sum[c], rcb);
-                        const float rr = __fmaf_rn(-(float)cnt, q0, sum[c]);
+                        const float rcb = __ldg(rcp + cn);
+                        const float q0 = __fmul_rn(sm, rcb);
+                        const float rr = __fmaf_rn(-cf, q0, sm);
                         key = __float_as_uint(__fmaf_rn(rr, rcb, q0));
                     } else {
-                        key = order_key(__fdiv_rn(sum[c], (float)cnt));
+                        key = order_key(__fdiv_rn(sm, cf));
                     }
                     if (key < best_key) {  // strict: the lowest d keeps ties
                         best_key = key;
@@ -513,7 +564,7 @@ __device__ __forceinline__ void vert_item(const ViewDesc &V, int x, int y0, int 
 }
 
 template <typename ST, int NCH, int POS>
-__global__ void __launch_bounds__(kVertT, NCH <= 4 ? 3 : 1)
+__global__ void __launch_bounds__(kVertT, NCH <= 4 ? 2 : 1)
     k_vert_views(ViewTable t, int L, int R, int DEP, const float *__restrict__ rcp) {
     constexpr int DM = 32 * NCH;  // ring row stride in entries
     extern __shared__ __align__(16) unsigned char vsm[];
@@ -708,7 +759,7 @@ rts_status launch_cross_views(rts_ctx *c, const rts_params &p, const ViewTable &
         const int nch = (max_d + 31) / 32;
         const int NCH = nch <= 1 ? 1 : nch <= 2 ? 2 : nch <= 4 ? 4 : 8;
         const size_t esz = half ? 4 : 8;
-        const size_t smem = (size_t)DEP * 32 * NCH * (esz + 2) + (size_t)DEP * 4;
+        const size_t smem = (size_t)DEP * 32 * NCH * (esz + 2) + (size_t)DEP * 4 + (size_t)32 * NCH * 4;
         const int R = tune.vert_rows;
         auto go = [&](auto kern) {
             cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
