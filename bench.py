@@ -413,6 +413,16 @@ def run_ours(args, rank, world):
 
     # parity spot check of this run's output against the last device run
     agree = bool(np.array_equal(ho[0].numpy(), o_dl.cpu().numpy()))
+    # FP16 form: share of disparities (both views) equal to the plain form's
+    f16_agree = None
+    if prec == R.PREC_F16:
+        p32 = R.params(cost1=c1, cost2=c2, aggr=ag, disp_range=D, precision=R.PREC_F32, **extra)
+        ref = [torch.empty((H, W), dtype=torch.uint8).pin_memory() for _ in range(3)]
+        rout = R.Out(ref[0].data_ptr(), ref[1].data_ptr(), ref[2].data_ptr(), None)
+        ctx.check(lib.rts_pipeline_run(ctx.h, R.HOST, C.byref(hpair), C.byref(p32), C.byref(rout)), "pipeline")
+        f16_agree = {"disp_left": float((ref[0].numpy() == ho[0].numpy()).mean()),
+                     "disp_right": float((ref[1].numpy() == ho[1].numpy()).mean()),
+                     "mask": float((ref[2].numpy() == ho[2].numpy()).mean())}
 
     if rank != 0:
         if world > 1:
@@ -420,7 +430,7 @@ def run_ours(args, rank, world):
         return
 
     peaks, src = measured_peaks()
-    roof = roofline(stages, name, W, H, D, ag, peaks, src, p)
+    roof = roofline(stages, name, W, H, D, ag, peaks, src, p, ms)
     line = {"metric": "MDE/s", "value": value, "unit": "MDE/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f16" if prec else "f32",
@@ -432,6 +442,7 @@ def run_ours(args, rank, world):
             "e2e": {"value": world * mde_pair / (e2e_ms / 1e3), "unit": "MDE/s", "ms_per_step": e2e_ms,
                     "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "host_equals_device_result": agree},
             "gpu_launches": launches, "wall_s": wall,
+            **({"f16_vs_f32_agreement": f16_agree} if f16_agree else {}),
             "stages_ms_per_step": {k: v[1] / args.steps for k, v in stages.items()},
             "roofline": roof, "clocks": clk.summary()}
     if not args.no_cpu:
@@ -446,40 +457,56 @@ def run_ours(args, rank, world):
         torch.distributed.destroy_process_group()
 
 
-def roofline(stages, name, W, H, D, ag, peaks, src, p):
-    """Dominant kernel and its algorithmic throughput."""
+# DRAM bytes per cost entry of the two cross-based kernels, from one ncu capture
+# of each at 1280x720, D=128 (both views; profiles/cross_views_*.md); a launch at
+# another size moves these per entry
+NCU_BYTES_PER_ENTRY = {("cross_vert_wta", 0): 4.16, ("cross_hseg", 0): 4.00}
+# ncu DRAM bytes of one k_aw_wta launch (one view) at 640x480, D=64 (profiles/k_aw_wta_*.md)
+NCU_AW_BYTES = {(640, 480, 64): 85.57e6}
+
+
+def roofline(stages, name, W, H, D, ag, peaks, src, p, ms_pair=None):
+    """Dominant kernel: algorithmic work per launch / its CUDA-event time, against
+    the measured peak; traffic = DRAM bytes per launch from ncu."""
     if not stages:
         return None
     dom = max(stages.items(), key=lambda kv: kv[1][1])
     kname, (launches, total_ms) = dom
     per_launch_ms = total_ms / max(1, launches)
-    E = W * H * D  # entries per view; each launch covers one view
+    E = W * H * D  # entries per view
     if kname == "aw_wta":
+        # one launch = one view; 4 FP32 operations per tap per entry (w = wR*wT, sum w,
+        # C*w, sum), the reference's order, unfused
         taps = (2 * p.aw_rad + 1) ** 2
-        flops = 4.0 * taps * E  # w = wR*wT, sum w, C*w, sum: 4 per tap per entry
+        flops = 4.0 * taps * E
         achieved = flops / (per_launch_ms / 1e3) / 1e12
         mhz = peaks.get("sm_max_mhz", 2070.0)
-        peak = 152 * 128 * 2 * mhz * 1e6 / 1e12  # FFMA lanes x 2 FLOP x clock
+        peak = 152 * 128 * mhz * 1e6 / 1e12  # one FP32 op per lane per clock (unfused ops)
+        traffic = NCU_AW_BYTES.get((W, H, D))
         return {"bound": "fp32", "kernel": "k_aw_wta", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                "frac": achieved / peak, "traffic": None, "launches": launches, "ms_per_launch": per_launch_ms,
+                "frac": achieved / peak, "traffic": traffic, "launches": launches, "ms_per_launch": per_launch_ms,
                 "flop_per_launch": flops,
-                "peak_source": f"FP32 FMA pipe: 152 SMs x 128 lanes x 2 FLOP x {mhz:.0f} MHz ({src} max clock); "
-                               "the plain form issues 4 unfused FP32 ops per tap, so 0.5 of this is its ceiling"}
-    # HBM-bound stages: compulsory bytes of the launch
+                "peak_source": f"FP32 pipe, unfused operations: 152 SMs x 128 lanes x {mhz:.0f} MHz "
+                               f"({src} max clock); no tensor-core or HBM bound applies (DRAM < 1% busy)"}
+    # HBM stage model (one launch = both views): the cost volume crosses HBM four
+    # times per view at S bytes an entry; the row-segment kernel owns the first two
+    # crossings (written by matching and combining, read by aggregation), the
+    # vertical kernel the last two (written by aggregation, read by WTA)
     S = 2 if p.precision else 4
-    if kname == "cross_hseg":
-        byts = S * E + 2 * 16 * W * H
-    elif kname == "cross_vert_wta":
-        byts = S * E + 2 * 16 * W * H + 2 * W * H
-    elif kname == "cost":
-        byts = S * E + 2 * 16 * W * H
-    else:
-        byts = S * E
+    views = 2
+    byts = views * 2 * S * E
     achieved = byts / (per_launch_ms / 1e3) / 1e9
     peak = peaks["hbm_gbs"]
-    return {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
-            "frac": achieved / peak, "traffic": None, "launches": launches, "ms_per_launch": per_launch_ms,
-            "bytes_per_launch": byts, "peak_source": src}
+    bpe = NCU_BYTES_PER_ENTRY.get((kname, 1 if p.precision else 0))
+    out = {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
+           "frac": achieved / peak, "traffic": bpe * views * E if bpe else None, "launches": launches,
+           "ms_per_launch": per_launch_ms, "bytes_per_launch": byts, "peak_source": src}
+    if ms_pair:
+        # the whole pair against the same model: 2 (4 S E) + 2 (2 W H + 6 W H) + 3 W H bytes
+        bp = 2 * (4 * S * E) + 2 * (8 * W * H) + 3 * W * H
+        out["pipeline"] = {"bytes_per_pair": bp, "achieved": bp / (ms_pair / 1e3) / 1e9,
+                           "frac": bp / (ms_pair / 1e3) / 1e9 / peak}
+    return out
 
 
 def main():

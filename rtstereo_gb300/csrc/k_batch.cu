@@ -396,7 +396,13 @@ __device__ __forceinline__ void vert_item(const ViewDesc &V, int x, int y0, int 
     // per disparity (shared): the target image column of column x
     int *tcs = reinterpret_cast<int *>(rinf + DEP);  // [DM]
     auto dok = [&](int c) { return 32 * c + lane < D; };
-    const In *segx = reinterpret_cast<const In *>(V.seg) + (size_t)x * D + lane;  // + r W D + 32 c
+    // the view's pointers, read once (the loops below store to shared memory, which
+    // the compiler might otherwise take to alias the view table)
+    const In *__restrict__ segx = reinterpret_cast<const In *>(V.seg) + (size_t)x * D + lane;  // + r W D + 32 c
+    const uint2 *__restrict__ arefx = V.aref + xsrc;  // + r W
+    const uint2 *__restrict__ atar = V.atar;
+    uint16_t *__restrict__ rawx = V.raw + x;  // + y W
+    int *__restrict__ rowl = V.row_last;
     const size_t segrow = (size_t)W * D;
     const int nticks = (rb - ra + 7) >> 3;
     // one tick's loads for this warp's row, in flight while the previous tick is used
@@ -405,8 +411,8 @@ __device__ __forceinline__ void vert_item(const ViewDesc &V, int x, int y0, int 
     auto load_tick = [&](int i) {
         const int r = ra + 8 * i + warp;
         if (r < rb) {
-            const uint2 *arow = V.atar + (size_t)r * W;
-            pref = V.aref[(size_t)r * W + xsrc];
+            const uint2 *arow = atar + (size_t)r * W;
+            pref = arefx[(size_t)r * W];
 #pragma unroll
             for (int c = 0; c < NC; c++) {
                 if (dok(c)) pseg[c] = segx[(size_t)r * segrow + 32 * c];
@@ -554,8 +560,8 @@ __device__ __forceinline__ void vert_item(const ViewDesc &V, int x, int y0, int 
             const uint32_t bd = __reduce_min_sync(0xffffffffu, best_key == m ? (uint32_t)best_d : 0xffffu);
             if (lane == 0) {
                 const bool found = bd != 0;  // some d >= 1 strictly below cost[0]
-                V.raw[(size_t)y * W + x] = found ? (uint16_t)(0x100 | bd) : (uint16_t)0;
-                if (found) atomicMax(V.row_last + y, x);
+                rawx[(size_t)y * W] = found ? (uint16_t)(0x100 | bd) : (uint16_t)0;
+                if (found) atomicMax(rowl + y, x);
             }
         }
         sbase += 8;
@@ -758,8 +764,9 @@ rts_status launch_cross_views(rts_ctx *c, const rts_params &p, const ViewTable &
         const int DEP = vert_depth(L);
         const int nch = (max_d + 31) / 32;
         const int NCH = nch <= 1 ? 1 : nch <= 2 ? 2 : nch <= 4 ? 4 : 8;
-        const size_t esz = half ? 4 : 8;
-        const size_t smem = (size_t)DEP * 32 * NCH * (esz + 2) + (size_t)DEP * 4 + (size_t)32 * NCH * 4;
+        // ring {segment, count} + arm words + reference arm words + target columns
+        const size_t DMb = (size_t)32 * NCH;
+        const size_t smem = (size_t)DEP * DMb * ((half ? 4 : 8) + 2) + (size_t)DEP * 4 + DMb * 4;
         const int R = tune.vert_rows;
         auto go = [&](auto kern) {
             cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
