@@ -99,12 +99,6 @@ __global__ void k_pack_lab(const uint8_t *__restrict__ lab, uint32_t *__restrict
     out[i] = (uint32_t)lab[3 * i] | ((uint32_t)lab[3 * i + 1] << 8) | ((uint32_t)lab[3 * i + 2] << 16);
 }
 
-__device__ __forceinline__ float lab_weight2(uint32_t c, uint32_t q, const float *__restrict__ G, float pwk) {
-    if ((q | c) & kLabOut) return 0.f;  // tap (or padding centre) outside the image
-    const uint32_t ad = __vabsdiffu4(c, q);
-    return __fmul_rn(pwk, __ldg(G + __dp4a(ad, ad, 0u)));
-}
-
 template <typename CT, bool EXACT>
 __global__ void __launch_bounds__(kAwThreads, 3) k_aw_wta(const CT *__restrict__ vol, const uint32_t *__restrict__ labr,
                                                       const uint32_t *__restrict__ labt, const float *__restrict__ pw,
@@ -203,21 +197,55 @@ __global__ void __launch_bounds__(kAwThreads, 3) k_aw_wta(const CT *__restrict__
             }
             __syncthreads();
             const float *pwrow = pw + (ky + r) * e;
-            for (int kx = warp; kx < e; kx += kAwThreads / 32) {
-                const float pwk = __ldg(pwrow + kx);
+            // weights of two taps per pass (kx and kx + 8), the table reads of both in
+            // flight together: the colour-distance index of every weight first, then the
+            // reads, then the products
+            for (int kx = warp; kx < e; kx += 2 * (kAwThreads / 32)) {
+                uint32_t idx[2][6];
+                bool ok[2][6];
 #pragma unroll
-                for (int m = 0; m < 2; m++) wRs[kx * kAwTX + lane + 32 * m] = lab_weight2(cR[m], labRrow[lane + 32 * m + kx], G, pwk);
+                for (int h = 0; h < 2; h++) {
+                    const int k = kx + h * (kAwThreads / 32);
 #pragma unroll
-                for (int m = 0; m < 4; m++) {
-                    const int u = lane + 32 * m;
-                    if (u < NT) {
-                        uint32_t q = labTrow[u + kx];
-                        if (wrapped_tile && tbase + u < 0) {
-                            // the target column is t + W: its tap is column t + W + kx - r
-                            const int xc = tbase + u + W + kx - r;
+                    for (int m = 0; m < 2; m++) {
+                        const uint32_t q = labRrow[imin(lane + 32 * m + k, kAwTX + 2 * r - 1)];
+                        ok[h][m] = k < e && !((q | cR[m]) & kLabOut);
+                        const uint32_t ad = __vabsdiffu4(cR[m], q);
+                        idx[h][m] = __dp4a(ad, ad, 0u);
+                    }
+#pragma unroll
+                    for (int m = 0; m < 4; m++) {
+                        const int u = lane + 32 * m;
+                        uint32_t q = labTrow[imin(u + k, NT + 2 * r - 1)];
+                        if (wrapped_tile && tbase + u < 0 && k < e) {
+                            // the target column is t + W: its tap is column t + W + k - r
+                            const int xc = tbase + u + W + k - r;
                             q = (xc >= 0 && xc < W) ? labt[crow + xc] : kLabOut;
                         }
-                        wTs[kx * NTP + u] = lab_weight2(cT[m], q, G, pwk);
+                        ok[h][2 + m] = k < e && u < NT && !((q | cT[m]) & kLabOut);
+                        const uint32_t ad = __vabsdiffu4(cT[m], q);
+                        idx[h][2 + m] = __dp4a(ad, ad, 0u);
+                    }
+                }
+                float g[2][6];
+#pragma unroll
+                for (int h = 0; h < 2; h++)
+#pragma unroll
+                    for (int m = 0; m < 6; m++) g[h][m] = ok[h][m] ? __ldg(G + idx[h][m]) : 0.f;
+#pragma unroll
+                for (int h = 0; h < 2; h++) {
+                    const int k = kx + h * (kAwThreads / 32);
+                    if (k < e) {
+                        // seq/AdaptiveWeightAggregation.cpp:33-71: pw[k] * expf(-dist / gamma_s),
+                        // 0 where the tap (or a padding centre) is outside the image
+                        const float pwk = __ldg(pwrow + k);
+#pragma unroll
+                        for (int m = 0; m < 2; m++) wRs[k * kAwTX + lane + 32 * m] = ok[h][m] ? __fmul_rn(pwk, g[h][m]) : 0.f;
+#pragma unroll
+                        for (int m = 0; m < 4; m++) {
+                            const int u = lane + 32 * m;
+                            if (u < NT) wTs[k * NTP + u] = ok[h][2 + m] ? __fmul_rn(pwk, g[h][2 + m]) : 0.f;
+                        }
                     }
                 }
             }
@@ -225,40 +253,51 @@ __global__ void __launch_bounds__(kAwThreads, 3) k_aw_wta(const CT *__restrict__
 
             // u index of wT for (j, i): px0 + j - 4td - i + 63 = ubase + (j - i) + 3
             const int ubase = px0 - 4 * td + kAwDC - 4;
-            const float *cbase = Cs + px0 * kAwCPitch + 4 * td;
-            // taps in groups of 4: the 7 cost columns px0+kx0 .. px0+kx0+6 of a group
-            // are loaded once and serve 4 pixels x 4 taps
+            const float *cp = Cs + px0 * kAwCPitch + 4 * td;  // cost column px0 + kx, + kx * pitch
+            const float *wrp = wRs + px0;                      // + kx * 64
+            const float *wtp = wTs + ubase;                    // + kx * NTP
+            // one tap: 4 pixels x 4 disparities, reference order per entry
+            auto tap = [&](const float (*cw)[4], int cofs, const float *wr4, const float *wt7) {
+                float wr[4], wt[7];
+                const float4 a0 = *reinterpret_cast<const float4 *>(wr4);
+                wr[0] = a0.x; wr[1] = a0.y; wr[2] = a0.z; wr[3] = a0.w;
+                const float4 b0 = *reinterpret_cast<const float4 *>(wt7);
+                const float4 b1 = *reinterpret_cast<const float4 *>(wt7 + 4);
+                wt[0] = b0.x; wt[1] = b0.y; wt[2] = b0.z; wt[3] = b0.w;
+                wt[4] = b1.x; wt[5] = b1.y; wt[6] = b1.z;
+#pragma unroll
+                for (int j = 0; j < 4; j++)
+#pragma unroll
+                    for (int i = 0; i < 4; i++) {
+                        const float w = __fmul_rn(wr[j], wt[j - i + 3]);
+                        sw[j][i] = __fadd_rn(sw[j][i], w);
+                        if constexpr (EXACT) sc[j][i] = __fadd_rn(sc[j][i], __fmul_rn(cw[j + cofs][i], w));
+                        else sc[j][i] = __fmaf_rn(cw[j + cofs][i], w, sc[j][i]);
+                    }
+            };
+            int kx = 0;
+            // taps in groups of 4: the 7 cost columns px0+kx .. px0+kx+6 of a group are
+            // loaded once and serve 4 pixels x 4 taps
 #pragma unroll 1
-            for (int kx0 = 0; kx0 < e; kx0 += 4) {
-                const int g = imin(4, e - kx0);
+            for (; kx + 4 <= e; kx += 4, cp += 4 * kAwCPitch, wrp += 4 * kAwTX, wtp += 4 * NTP) {
                 float cw[7][4];
 #pragma unroll
                 for (int q = 0; q < 7; q++) {
-                    const float4 v = *reinterpret_cast<const float4 *>(cbase + (kx0 + q) * kAwCPitch);
+                    const float4 v = *reinterpret_cast<const float4 *>(cp + q * kAwCPitch);
                     cw[q][0] = v.x; cw[q][1] = v.y; cw[q][2] = v.z; cw[q][3] = v.w;
                 }
 #pragma unroll
-                for (int u = 0; u < 4; u++) {
-                    if (u < g) {
-                        const int kx = kx0 + u;
-                        float wr[4], wt[7];
-                        const float4 a0 = *reinterpret_cast<const float4 *>(wRs + kx * kAwTX + px0);
-                        wr[0] = a0.x; wr[1] = a0.y; wr[2] = a0.z; wr[3] = a0.w;
-                        const float4 *wp = reinterpret_cast<const float4 *>(wTs + kx * NTP + ubase);
-                        const float4 b0 = wp[0], b1 = wp[1];
-                        wt[0] = b0.x; wt[1] = b0.y; wt[2] = b0.z; wt[3] = b0.w;
-                        wt[4] = b1.x; wt[5] = b1.y; wt[6] = b1.z;
+                for (int u = 0; u < 4; u++) tap(cw, u, wrp + u * kAwTX, wtp + u * NTP);
+            }
+#pragma unroll 1
+            for (; kx < e; kx++, cp += kAwCPitch, wrp += kAwTX, wtp += NTP) {
+                float cw[4][4];
 #pragma unroll
-                        for (int j = 0; j < 4; j++)
-#pragma unroll
-                            for (int i = 0; i < 4; i++) {
-                                const float w = __fmul_rn(wr[j], wt[j - i + 3]);
-                                sw[j][i] = __fadd_rn(sw[j][i], w);
-                                if constexpr (EXACT) sc[j][i] = __fadd_rn(sc[j][i], __fmul_rn(cw[j + u][i], w));
-                                else sc[j][i] = __fmaf_rn(cw[j + u][i], w, sc[j][i]);
-                            }
-                    }
+                for (int q = 0; q < 4; q++) {
+                    const float4 v = *reinterpret_cast<const float4 *>(cp + q * kAwCPitch);
+                    cw[q][0] = v.x; cw[q][1] = v.y; cw[q][2] = v.z; cw[q][3] = v.w;
                 }
+                tap(cw, 0, wrp, wtp);
             }
         }
         __syncthreads();
