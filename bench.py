@@ -41,6 +41,9 @@ WORKLOADS = {
     "cross_1280x720_d128": (1280, 720, 128, 1, 3, 3, 24, 2, 3.0, 0xC2, {}),
     "aw_1920x1080_d128": (1920, 1080, 128, 1, 3, 2, 24, 2, 3.0, 0xC2, {}),
     "rank_census_cross_1920x1080_d128": (1920, 1080, 128, 2, 3, 3, 24, 2, 3.0, 0xC2, {"rank_rad": 3}),
+    "box_1920x1080_d128": (1920, 1080, 128, 1, 3, 1, 24, 2, 3.0, 0xC2, {"box_rad": 4}),
+    "ncc_box_1920x1080_d128": (1920, 1080, 128, 5, 0, 1, 24, 2, 3.0, 0xC2, {"box_rad": 4, "ncc_hrad": 3,
+                                                                            "ncc_wrad": 3}),
 }
 DEFAULT = "aw_640x480_d64"
 

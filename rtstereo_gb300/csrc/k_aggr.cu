@@ -24,6 +24,109 @@ __global__ void k_box(const float *__restrict__ in, float *__restrict__ out, int
     out[((size_t)y * W + x) * D + d] = __fdiv_rn(s, (float)((2 * r + 1) * (2 * r + 1)));
 }
 
+// Box mean and arg-min in one pass (the out-of-place box of
+// seq/ConstBlockAggregation.cpp:11-34 followed by seq/WTA.cpp:10-39).  Block per
+// (32 x 8 pixel tile, 32 disparities): the tile and its R-pixel wrapped border
+// are staged in shared memory, lane = disparity; a warp takes one row of the
+// tile in groups of 8 pixels, so every staged row of 8 + 2R values feeds
+// 8 x (2R + 1) adds.  Each sum is the reference's single chain, rows outer and
+// columns inner.  The winner of the block's 32 disparities enters a per-pixel
+// 64-bit minimum {key << 32 | d}: the key orders like the reference's strict
+// comparisons (a NaN never wins, a NaN at d = 0 blocks every other d, -0 == +0).
+constexpr int kBoxTX = 32, kBoxTY = 8;
+
+__device__ __forceinline__ uint32_t wta_key(float v, int d, int argmax) {
+    if (v != v) return d == 0 ? 0u : 0xffffffffu;
+    uint32_t u = __float_as_uint(__fadd_rn(v, 0.0f));  // -0 -> +0
+    u = (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+    return argmax ? ~u : u;
+}
+
+template <int R, int POS>
+__global__ void __launch_bounds__(256) k_box_best(const float *__restrict__ vol, unsigned long long *__restrict__ best,
+                                                  int H, int W, int D, int argmax, float rcp_area) {
+    constexpr int TW = kBoxTX + 2 * R, TH = kBoxTY + 2 * R, AREA = (2 * R + 1) * (2 * R + 1);
+    constexpr int G = 16;  // pixels of a thread's group
+    extern __shared__ float bt[];  // [TH][TW][32]
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int x0 = blockIdx.x * kBoxTX, y0 = blockIdx.y * kBoxTY, d = blockIdx.z * 32 + lane;
+    // the tile rows, every cell in flight at once (cp.async, zero fill past D); single
+    // wrap as in seq/ConstBlockAggregation.cpp:19-24 (R < H, R < W); rows and columns
+    // past the last pixel's window are never read and are clamped into range
+    const bool inner = x0 >= R && x0 + kBoxTX + R <= W;
+    const int dofs = d < D ? d : 0;
+    const unsigned nbytes = d < D ? 4u : 0u;
+    for (int i = warp; i < TH; i += 8) {
+        const int yy = wrap1(imin(y0 - R + i, H - 1 + R), H);
+        const float *rowp = vol + (size_t)yy * W * D + dofs;
+        unsigned dst = (unsigned)__cvta_generic_to_shared(bt + i * TW * 32 + lane);
+        if (inner) {
+            const float *src = rowp + (size_t)(x0 - R) * D;
+#pragma unroll 8
+            for (int j = 0; j < TW; j++, src += D, dst += 128)
+                asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(dst), "l"(src), "r"(nbytes)
+                             : "memory");
+        } else {
+            for (int j = 0; j < TW; j++, dst += 128) {
+                const int xx = wrap1(imin(x0 - R + j, W - 1 + R), W);
+                asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(dst),
+                             "l"(rowp + (size_t)xx * D), "r"(nbytes)
+                             : "memory");
+            }
+        }
+    }
+    asm volatile("cp.async.wait_all;\n" ::: "memory");
+    __syncthreads();
+    const int y = y0 + warp;
+    if (y >= H) return;
+#pragma unroll 1
+    for (int g = 0; g < kBoxTX / G; g++) {
+        float sm[G];
+#pragma unroll
+        for (int j = 0; j < G; j++) sm[j] = 0.f;
+#pragma unroll
+        for (int dy = 0; dy <= 2 * R; dy++) {
+            float v[G + 2 * R];
+            const float *rp = bt + ((warp + dy) * TW + G * g) * 32 + lane;
+#pragma unroll
+            for (int k = 0; k < G + 2 * R; k++) v[k] = rp[k * 32];
+#pragma unroll
+            for (int j = 0; j < G; j++)
+#pragma unroll
+                for (int dx = 0; dx <= 2 * R; dx++) sm[j] = __fadd_rn(sm[j], v[j + dx]);
+        }
+#pragma unroll
+        for (int j = 0; j < G; j++) {
+            const int x = x0 + G * g + j;
+            float q;
+            if (POS) {
+                // non-negative sums of costs >= 0: the correctly rounded quotient by
+                // Markstein's correction from the correctly rounded 1 / AREA
+                const float q0 = __fmul_rn(sm[j], rcp_area);
+                q = __fmaf_rn(__fmaf_rn(-(float)AREA, q0, sm[j]), rcp_area, q0);
+            } else {
+                q = __fdiv_rn(sm[j], (float)AREA);  // seq/ConstBlockAggregation.cpp:31
+            }
+            const uint32_t key = d < D ? wta_key(q, d, argmax) : 0xffffffffu;
+            const uint32_t m = __reduce_min_sync(0xffffffffu, key);
+            const uint32_t bd = __reduce_min_sync(0xffffffffu, key == m ? (uint32_t)d : 0xffffffffu);
+            if (lane == 0 && x < W) atomicMin(best + (size_t)y * W + x, ((unsigned long long)m << 32) | bd);
+        }
+    }
+}
+
+// per-pixel minimum -> WTA winner word and row summary (see k_wta.cu)
+__global__ void k_best_raw(const unsigned long long *__restrict__ best, uint16_t *__restrict__ raw,
+                           int *__restrict__ row_last, int H, int W) {
+    const int y = blockIdx.y;
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= W) return;
+    const int win = (int)(best[(size_t)y * W + x] & 0xffffffffu);
+    const bool found = win != 0;  // some d >= 1 strictly better than d = 0
+    raw[(size_t)y * W + x] = found ? (uint16_t)(0x100 | win) : (uint16_t)0;
+    if (found) atomicMax(row_last + y, x);
+}
+
 // One cross arm (seq/CrossBasedAggregation.cpp:12-100): step outward while the
 // last visited pixel differs from the centre by < tau in every channel and the
 // arm is shorter than L; the first failing pixel is included; stop at the edge.
@@ -203,6 +306,35 @@ static dim3 row_grid(long per_row, int H, int threads) { return dim3((unsigned)(
 
 void launch_box(cudaStream_t s, const float *in, float *out, int H, int W, int D, int r) {
     k_box<<<row_grid((long)W * D, H, 256), 256, 0, s>>>(in, out, H, W, D, r);
+}
+bool box_best_supported(int r) { return r >= 1 && r <= 8; }
+void launch_box_best(cudaStream_t s, const float *vol, unsigned long long *best, uint16_t *raw, int *row_last, int H,
+                     int W, int D, int r, int argmax, int pos) {
+    const dim3 g((W + kBoxTX - 1) / kBoxTX, (H + kBoxTY - 1) / kBoxTY, (D + 31) / 32);
+    const int area = (2 * r + 1) * (2 * r + 1);
+    const float rcp_area = 1.0f / (float)area;  // host IEEE division: correctly rounded
+    auto go = [&](auto kern, int R) {
+        const size_t smem = (size_t)(kBoxTX + 2 * R) * (kBoxTY + 2 * R) * 32 * sizeof(float);
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        kern<<<g, 256, smem, s>>>(vol, best, H, W, D, argmax, rcp_area);
+    };
+#define RTS_BOX(RR)                                \
+    case RR:                                       \
+        if (pos) go(k_box_best<RR, 1>, RR);        \
+        else go(k_box_best<RR, 0>, RR);            \
+        break;
+    switch (r) {
+        RTS_BOX(1)
+        RTS_BOX(2)
+        RTS_BOX(3)
+        RTS_BOX(4)
+        RTS_BOX(5)
+        RTS_BOX(6)
+        RTS_BOX(7)
+        RTS_BOX(8)
+    }
+#undef RTS_BOX
+    k_best_raw<<<row_grid(W, H, 256), 256, 0, s>>>(best, raw, row_last, H, W);
 }
 void launch_find_cross(cudaStream_t s, const uint8_t *rgb, int *horz, int *vert, int H, int W, int L, int tau) {
     k_find_cross<<<row_grid(W, H, 128), 128, 0, s>>>(rgb, horz, vert, H, W, L, tau);

@@ -160,6 +160,12 @@ void launch_combine(cudaStream_t s, float *c1, const float *c2, long n, const fl
                     float lambda1, float lambda2);
 // k_aggr.cu
 void launch_box(cudaStream_t s, const float *in, float *out, int H, int W, int D, int r);
+// box mean + WTA winners in one pass (radius 1..8): best[] must hold all ones;
+// writes raw / row_last as launch_wta_local does (two launches); pos: every cost
+// is >= 0 (the fast exact division applies)
+bool box_best_supported(int r);
+void launch_box_best(cudaStream_t s, const float *vol, unsigned long long *best, uint16_t *raw, int *row_last, int H,
+                     int W, int D, int r, int argmax, int pos);
 void launch_find_cross(cudaStream_t s, const uint8_t *rgb, int *horz, int *vert, int H, int W, int L, int tau);
 void launch_prefix_h(cudaStream_t s, float *cost, int H, int W, int D);
 void launch_cross_aggr(cudaStream_t s, const float *pre, float *out, const int *hr, const int *ht, const int *vr,

@@ -146,7 +146,17 @@ static rts_status view_composed(rts_ctx *c, const rts_params &p, int H, int W, c
     void *c1v, *finv = nullptr;
     RTS_TRY(scratch(c, SL_V_COST1, ne * 4, &c1v));
     float *c1 = (float *)c1v;
-    {
+    const bool box_pass = p.aggr == RTS_AGGR_BOX && !cost_out && box_best_supported(p.box_rad);
+    if (box_pass && fast_costs(p)) {
+        // AD / census costs of the box pass: one volume pass from per-pixel records
+        StageScope sc(c, "cost");
+        void *recv;
+        RTS_TRY(scratch(c, SL_V_REC, np * 32, &recv));
+        uint4 *rr = (uint4 *)recv, *rt = rr + np;
+        RTS_TRY(prep_records(c, p, H, W, v.gref, v.cref, rr, nullptr));
+        RTS_TRY(prep_records(c, p, H, W, v.gtar, v.ctar, rt, nullptr));
+        RTS_TRY(cost_volume_fast(c, p, H, W, rr, rt, c1, 0));
+    } else {
         StageScope sc(c, "cost");
         RTS_TRY(one_cost(c, p, p.cost1, p.aggr == RTS_AGGR_CROSS, H, W, v, c1, SL_V_AUX));
         if (p.cost2 != RTS_COST_NONE) {
@@ -160,6 +170,30 @@ static rts_status view_composed(rts_ctx *c, const rts_params &p, int H, int W, c
         }
     }
     float *fin = c1;
+    const int argmax = (p.cost1 == RTS_COST_NCC && p.cost2 == RTS_COST_NONE) ? 1 : 0;
+    if (box_pass) {
+        // box mean and arg-min in one pass over the volume
+        void *raw, *rl, *bestv;
+        RTS_TRY(scratch(c, SL_V_RAW, np * 2, &raw));
+        RTS_TRY(scratch(c, SL_V_ROWLAST, (size_t)H * 4, &rl));
+        RTS_TRY(scratch(c, SL_V_SEG, np * 8, &bestv));
+        {
+            StageScope sc(c, "box_wta");
+            RTS_CU(c, cudaMemsetAsync(rl, 0xff, (size_t)H * 4, s));
+            RTS_CU(c, cudaMemsetAsync(bestv, 0xff, np * 8, s));
+            // every cost but NCC is >= 0 (absolute differences, distances, 1 - exp(-c/l))
+            const bool pos = p.cost1 != RTS_COST_NCC;
+            launch_box_best(s, c1, (unsigned long long *)bestv, (uint16_t *)raw, (int *)rl, H, W, D, p.box_rad, argmax,
+                            pos ? 1 : 0);
+            count_launch(c, 2);
+        }
+        {
+            StageScope sc(c, "wta_fill");
+            launch_wta_fill(s, (const uint16_t *)raw, (const int *)rl, disp, H, W, mirror);
+            count_launch(c);
+        }
+        return check_launch(c, "pipeline view");
+    }
     if (p.aggr == RTS_AGGR_BOX) {
         StageScope sc(c, "box");
         RTS_TRY(scratch(c, SL_V_SEG, ne * 4, &finv));
@@ -200,7 +234,6 @@ static rts_status view_composed(rts_ctx *c, const rts_params &p, int H, int W, c
         RTS_TRY(scratch(c, SL_V_RAW, np * 2, &raw));
         RTS_TRY(scratch(c, SL_V_ROWLAST, (size_t)H * 4, &rl));
         RTS_CU(c, cudaMemsetAsync(rl, 0xff, (size_t)H * 4, s));
-        const int argmax = (p.cost1 == RTS_COST_NCC && p.cost2 == RTS_COST_NONE) ? 1 : 0;
         launch_wta_local(s, fin, (uint16_t *)raw, (int *)rl, H, W, D, argmax);
         launch_wta_fill(s, (const uint16_t *)raw, (const int *)rl, disp, H, W, mirror);
         count_launch(c, 2);
