@@ -121,6 +121,33 @@ __global__ void k_pack_lab(const uint8_t *__restrict__ lab, uint32_t *__restrict
     out[i] = (uint32_t)lab[3 * i] | ((uint32_t)lab[3 * i + 1] << 8) | ((uint32_t)lab[3 * i + 2] << 16);
 }
 
+// packed pairs of floats for the f32x2 instructions
+__device__ __forceinline__ unsigned long long pack2(float lo, float hi) {
+    unsigned long long r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
+}
+__device__ __forceinline__ float half2_of(unsigned long long v, int hi) {
+    float lo_, hi_;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo_), "=f"(hi_) : "l"(v));
+    return hi ? hi_ : lo_;
+}
+__device__ __forceinline__ unsigned long long add2(unsigned long long a, unsigned long long b) {
+    unsigned long long r;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ unsigned long long mul2(unsigned long long a, unsigned long long b) {
+    unsigned long long r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ unsigned long long fma2(unsigned long long a, unsigned long long b, unsigned long long c) {
+    unsigned long long r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+    return r;
+}
+
 template <typename CT, bool EXACT>
 __global__ void __launch_bounds__(kAwThreads, 3) k_aw_wta(const CT *__restrict__ vol, const uint32_t *__restrict__ labr,
                                                       const uint32_t *__restrict__ labt, const float *__restrict__ pw,
@@ -151,11 +178,13 @@ __global__ void __launch_bounds__(kAwThreads, 3) k_aw_wta(const CT *__restrict__
     const bool vec = (D & 3) == 0;
 
     for (int dc0 = 0; dc0 < D; dc0 += kAwDC) {
-        float sw[4][4], sc[4][4];
+        // sums of disparity pairs (4td + 2h, 4td + 2h + 1) of pixel px0 + j, packed for
+        // the f32x2 instructions (each half an IEEE round-to-nearest operation)
+        unsigned long long sw[4][2], sc[4][2];
 #pragma unroll
         for (int j = 0; j < 4; j++)
 #pragma unroll
-            for (int i = 0; i < 4; i++) sw[j][i] = sc[j][i] = 0.f;
+            for (int h = 0; h < 2; h++) sw[j][h] = sc[j][h] = 0ull;
         // centre Lab words: reference pixels x0+lane+32m, target columns t(u), u = lane+32m
         const int tbase = x0 - dc0 - (kAwDC - 1);  // target column of u = 0, before wrapping
         uint32_t cR[2], cT[4];
@@ -290,11 +319,14 @@ __global__ void __launch_bounds__(kAwThreads, 3) k_aw_wta(const CT *__restrict__
 #pragma unroll
                 for (int j = 0; j < 4; j++)
 #pragma unroll
-                    for (int i = 0; i < 4; i++) {
-                        const float w = __fmul_rn(wr[j], wt[j - i + 3]);
-                        sw[j][i] = __fadd_rn(sw[j][i], w);
-                        if constexpr (EXACT) sc[j][i] = __fadd_rn(sc[j][i], __fmul_rn(cw[j + cofs][i], w));
-                        else sc[j][i] = __fmaf_rn(cw[j + cofs][i], w, sc[j][i]);
+                    for (int h = 0; h < 2; h++) {
+                        // w of disparities i = 2h, 2h+1: wR * wT (index j - i + 3)
+                        const unsigned long long w = pack2(__fmul_rn(wr[j], wt[j - 2 * h + 3]),
+                                                           __fmul_rn(wr[j], wt[j - 2 * h + 2]));
+                        const unsigned long long c = pack2(cw[j + cofs][2 * h], cw[j + cofs][2 * h + 1]);
+                        sw[j][h] = add2(sw[j][h], w);
+                        if constexpr (EXACT) sc[j][h] = add2(sc[j][h], mul2(c, w));
+                        else sc[j][h] = fma2(c, w, sc[j][h]);
                     }
             };
             int kx = 0;
@@ -329,7 +361,7 @@ __global__ void __launch_bounds__(kAwThreads, 3) k_aw_wta(const CT *__restrict__
         for (int j = 0; j < 4; j++)
 #pragma unroll
             for (int i = 0; i < 4; i++) {
-                const float v = __fdiv_rn(sc[j][i], sw[j][i]);
+                const float v = __fdiv_rn(half2_of(sc[j][i >> 1], i & 1), half2_of(sw[j][i >> 1], i & 1));
                 outs[(px0 + j) * (kAwDC + 1) + 4 * td + i] = v;
                 const int x = x0 + px0 + j, dg = dc0 + 4 * td + i;
                 if (cost_out && x < W && dg < D) cost_out[((size_t)y * W + x) * D + dg] = v;
