@@ -23,9 +23,11 @@
 // window, and its wrap at the borders, are mirror symmetric), so every Hamming
 // distance is the same.  The per-entry arithmetic is the reference's, so a
 // pair's result does not depend on what else is in the batch.
+#include <algorithm>
 #include <type_traits>
 
 #include "rts_fused.cuh"
+#include "rts_pipe.h"
 #include "rts_views.h"
 
 namespace rts {
@@ -48,20 +50,25 @@ __device__ __forceinline__ int find_view(const int *__restrict__ off, int n, int
 constexpr int kPrepTW = 64, kPrepTH = 16, kPrepT = 256;
 constexpr uint32_t kNoPixel = 0xff000000u;
 
-static size_t prep_smem(int hr, int wr, int L) {
-    return (size_t)4 * (kPrepTW + 2 * L) * (kPrepTH + 2 * L) + (size_t)(kPrepTH + 2 * hr) * (kPrepTW + 2 * wr);
+static size_t prep_smem(int gr, int gc, int L) {
+    return (size_t)4 * (kPrepTW + 2 * L) * (kPrepTH + 2 * L) + (size_t)(kPrepTH + 2 * gr) * (kPrepTW + 2 * gc);
 }
 
 // GRAYREC: the record colour is the gray byte (all views of the launch are
 // gray; the cost kernel then takes 3|dI| as the colour AD), else packed RGB with
-// gray replicated into the three channels (seq/Main.cpp:87-90)
+// gray replicated into the three channels (seq/Main.cpp:87-90).  rank >= 0: the
+// record's colour word holds the rank of the pixel instead (radius rank,
+// seq/RankFilter.cpp:11-35), which a mirrored view reads unchanged (the window
+// and its wrap are mirror symmetric).  The gray tile has a wrapped border of
+// gr rows and gc columns (the larger of the census and rank windows).
 template <int GRAYREC>
-__global__ void __launch_bounds__(kPrepT) k_prep_views(ViewTable t, int hr, int wr, int L, int tau, int want_code) {
+__global__ void __launch_bounds__(kPrepT) k_prep_views(ViewTable t, int hr, int wr, int L, int tau, int want_code,
+                                                       int rank, int gr, int gc) {
     extern __shared__ __align__(16) unsigned char psm[];
     const int nv = t.nviews;
     const int *off = t.off + ST_PREP * (nv + 1);
     const int cw = kPrepTW + 2 * L, chh = kPrepTH + 2 * L;
-    const int gw = kPrepTW + 2 * wr, gh = kPrepTH + 2 * hr;
+    const int gw = kPrepTW + 2 * gc, gh = kPrepTH + 2 * gr;
     uint32_t *ct = reinterpret_cast<uint32_t *>(psm);  // [chh][cw] colours
     uint8_t *gt = psm + (size_t)4 * cw * chh;          // [gh][gw] gray, wrapped
     for (int item = blockIdx.x; item < t.total[ST_PREP]; item += gridDim.x) {
@@ -95,13 +102,13 @@ __global__ void __launch_bounds__(kPrepT) k_prep_views(ViewTable t, int hr, int 
             }
             ct[q] = col;
         }
-        if (want_code)
+        if (want_code || rank >= 0)
             for (int q = threadIdx.x; q < gw * gh; q += kPrepT) {
                 const int r = q / gw, cx = q - r * gw;
                 // rows / columns past the last pixel's window are never read; clamp them
-                // into the single-wrap range (hr < H, wr < W)
-                const int yy = wrap1(imin(y0 - hr + r, H - 1 + hr), H);
-                const int xx = wrap1(imin(x0 - wr + cx, W - 1 + wr), W);
+                // into the single-wrap range (the window radii are below H and W)
+                const int yy = wrap1(imin(y0 - gr + r, H - 1 + gr), H);
+                const int xx = wrap1(imin(x0 - gc + cx, W - 1 + gc), W);
                 gt[q] = gray[(size_t)yy * W + xx];
             }
         __syncthreads();
@@ -112,7 +119,7 @@ __global__ void __launch_bounds__(kPrepT) k_prep_views(ViewTable t, int hr, int 
             uint32_t lo = 0, hi = 0;
             if (want_code) {
                 // seq/CensusTransform.cpp:11-37: bit (dy+hr)*(2wr+1)+(dx+wr), strict centre > neighbour
-                const uint8_t *g0 = gt + py * gw + px;
+                const uint8_t *g0 = gt + (py + gr - hr) * gw + px + gc - wr;
                 const uint32_t c = g0[hr * gw + wr];
                 int k = 0;
                 for (int r = 0; r <= 2 * hr; r++)
@@ -147,7 +154,17 @@ __global__ void __launch_bounds__(kPrepT) k_prep_views(ViewTable t, int hr, int 
             const uint32_t lr = (uint32_t)len[0] | ((uint32_t)len[1] << 16);
             const uint32_t tb = (uint32_t)len[2] | ((uint32_t)len[3] << 16);
             const size_t p = (size_t)y * W + x;
-            rec[p] = make_uint4(lo, hi, centre, lr);
+            uint32_t cword = centre;
+            if (rank >= 0) {
+                // seq/RankFilter.cpp:16-29: 1 + neighbours strictly below the centre, as u8
+                const uint8_t *g0 = gt + (py + gr - rank) * gw + px + gc - rank;
+                const uint32_t c = g0[rank * gw + rank];
+                int cnt = 1;
+                for (int r = 0; r <= 2 * rank; r++)
+                    for (int dx = 0; dx <= 2 * rank; dx++) cnt += (uint32_t)g0[r * gw + dx] < c ? 1 : 0;
+                cword = (uint32_t)(uint8_t)cnt;
+            }
+            rec[p] = make_uint4(lo, hi, cword, lr);
             arm[p] = make_uint2(lr, tb);
         }
     }
@@ -239,7 +256,10 @@ __global__ void __launch_bounds__(kHsegW * 32, 8) k_hseg_views(ViewTable t, Cost
                     } else if constexpr (MODE == 1) {
                         // CombineCost of min(SAD, trunc) and the Hamming distance: one host-made
                         // table of T1[s] + T2[h] (seq/CombineCost.cpp:21-23)
-                        int s = GRAYREC ? abs((int)a.z - (int)b.z) * 3 : (int)__vsadu4(a.z, b.z);
+                        // the first cost: colour AD (truncated), or the AD of the ranks
+                        // (seq/PixelBasedCost.cpp:13-24 on rank images)
+                        int s = GRAYREC == 2 ? abs((int)a.z - (int)b.z)
+                                : GRAYREC ? abs((int)a.z - (int)b.z) * 3 : (int)__vsadu4(a.z, b.z);
                         s = imin(s, cfg.itrunc);
                         const int hd = __popc(a.x ^ b.x) + __popc(a.y ^ b.y);
                         cv[u] = __ldg(lut2d + s * 65 + hd);
@@ -681,14 +701,24 @@ template <typename K> static int resident_blocks(K kern, int threads, size_t sme
 }
 
 static bool mode1(const rts_params &p) {
-    // AD (truncated, seq/Main.cpp:183-186) + census with an integral truncation
-    return p.cost1 == RTS_COST_AD && p.cost2 == RTS_COST_CENSUS && p.ad_trunc >= 0.f &&
-           p.ad_trunc < (float)kCombineLut && p.ad_trunc == floorf(p.ad_trunc);
+    // AD (truncated, seq/Main.cpp:183-186) with an integral truncation, or rank
+    // differences, combined with census: integer costs through one host table
+    const bool ad = p.cost1 == RTS_COST_AD && p.ad_trunc >= 0.f && p.ad_trunc < (float)kCombineLut &&
+                    p.ad_trunc == floorf(p.ad_trunc);
+    return (ad || (p.cost1 == RTS_COST_RANK && p.rank_rad <= 16)) && p.cost2 == RTS_COST_CENSUS;
+}
+// the largest first-cost value of the table path
+static int mode1_smax(const rts_params &p) { return p.cost1 == RTS_COST_RANK ? 255 : (int)p.ad_trunc; }
+
+bool cross_record_costs(const rts_params &p) {
+    if (!mode1(p) && !fast_costs(p)) return false;
+    const bool census = p.cost1 == RTS_COST_CENSUS || p.cost2 == RTS_COST_CENSUS;
+    return !census || (2 * p.census_hrad + 1) * (2 * p.census_wrad + 1) <= 64;
 }
 
 rts_status cross_tables(rts_ctx *c, const rts_params &p) {
     const float *t;
-    if (mode1(p)) RTS_TRY(combine_lut2d(c, p.lambda1, p.lambda2, (int)p.ad_trunc, &t));
+    if (mode1(p)) RTS_TRY(combine_lut2d(c, p.lambda1, p.lambda2, mode1_smax(p), &t));
     else if (p.cost2 != RTS_COST_NONE) {
         const float *t2;
         RTS_TRY(combine_luts(c, p.lambda1, p.lambda2, &t, &t2));
@@ -715,10 +745,14 @@ rts_status launch_cross_views(rts_ctx *c, const rts_params &p, const ViewTable &
     cfg.itrunc = cfg.trunc1 ? (int)p.ad_trunc : 0x7fffffff;
     const int mode = has_vol ? 0 : mode1(p) ? 1 : 2;
     const float *lut2d = nullptr, *rcp = nullptr;
-    if (mode == 1) RTS_TRY(combine_lut2d(c, p.lambda1, p.lambda2, (int)p.ad_trunc, &lut2d));
-    else if (p.cost2 != RTS_COST_NONE) RTS_TRY(combine_luts(c, p.lambda1, p.lambda2, &cfg.lut1, &cfg.lut2));
+    if (mode == 1) {
+        RTS_TRY(combine_lut2d(c, p.lambda1, p.lambda2, mode1_smax(p), &lut2d));
+        cfg.itrunc = mode1_smax(p);
+    } else if (p.cost2 != RTS_COST_NONE) RTS_TRY(combine_luts(c, p.lambda1, p.lambda2, &cfg.lut1, &cfg.lut2));
     RTS_TRY(recip_table(c, &rcp));
-    const int grayrec = (mode == 1 && gray) ? 1 : 0;
+    const bool rank = mode == 1 && p.cost1 == RTS_COST_RANK;
+    // record colour word: 2 rank, 1 gray byte, 0 packed RGB
+    const int grayrec = rank ? 2 : (mode == 1 && gray) ? 1 : 0;
     cudaStream_t s = c->stream;
     const int sms = num_sms();
     auto grid = [&](int items, int per_block, int per_sm) {
@@ -732,13 +766,15 @@ rts_status launch_cross_views(rts_ctx *c, const rts_params &p, const ViewTable &
     if (t.total[ST_PREP] > 0) {
         StageScope sc(c, "prep");
         const int hr = want_code ? p.census_hrad : 0, wr = want_code ? p.census_wrad : 0;
-        const size_t smem = prep_smem(hr, wr, L);
+        const int rk = rank ? p.rank_rad : -1;
+        const int gr = std::max(hr, std::max(rk, 0)), gc = std::max(wr, std::max(rk, 0));
+        const size_t smem = prep_smem(gr, gc, L);
         auto go = [&](auto kern) {
             cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
             kern<<<grid(t.total[ST_PREP], 1, resident_blocks(kern, kPrepT, smem)), kPrepT, smem, s>>>(
-                t, hr, wr, L, p.cross_tau, want_code ? 1 : 0);
+                t, hr, wr, L, p.cross_tau, want_code ? 1 : 0, rk, gr, gc);
         };
-        if (grayrec) go(k_prep_views<1>);
+        if (grayrec == 1) go(k_prep_views<1>);
         else go(k_prep_views<0>);
         count_launch(c);
     }
@@ -748,12 +784,14 @@ rts_status launch_cross_views(rts_ctx *c, const rts_params &p, const ViewTable &
         auto go = [&](auto kern) { kern<<<g, kHsegW * 32, 0, s>>>(t, cfg, lut2d); };
         if (half) {
             if (mode == 0) go(k_hseg_views<__half, 0, 0>);
-            else if (mode == 1 && grayrec) go(k_hseg_views<__half, 1, 1>);
+            else if (mode == 1 && grayrec == 2) go(k_hseg_views<__half, 1, 2>);
+            else if (mode == 1 && grayrec == 1) go(k_hseg_views<__half, 1, 1>);
             else if (mode == 1) go(k_hseg_views<__half, 1, 0>);
             else go(k_hseg_views<__half, 2, 0>);
         } else {
             if (mode == 0) go(k_hseg_views<float, 0, 0>);
-            else if (mode == 1 && grayrec) go(k_hseg_views<float, 1, 1>);
+            else if (mode == 1 && grayrec == 2) go(k_hseg_views<float, 1, 2>);
+            else if (mode == 1 && grayrec == 1) go(k_hseg_views<float, 1, 1>);
             else if (mode == 1) go(k_hseg_views<float, 1, 0>);
             else go(k_hseg_views<float, 2, 0>);
         }

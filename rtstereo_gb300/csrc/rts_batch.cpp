@@ -133,7 +133,7 @@ rts_status rts_batch_run(rts_ctx *ctx, int n, const rts_pair *pairs, const rts_p
     std::lock_guard<std::recursive_mutex> lk(ctx->mu);
     rts_ctx *c = ctx;
     if (cudaSetDevice(c->device) != cudaSuccess) return set_error(c, RTS_ERR_CUDA, "cudaSetDevice failed");
-    bool batched = params[0].aggr == RTS_AGGR_CROSS && cross_fused_supported(params[0]) && fast_costs(params[0]);
+    bool batched = params[0].aggr == RTS_AGGR_CROSS && cross_fused_supported(params[0]) && cross_record_costs(params[0]);
     for (int i = 0; i < n && batched; i++) {
         RTS_TRY(validate_params(c, params[i], pairs[i].height, pairs[i].width));
         batched = same_except_d(params[0], params[i]) && cross_fused_supported(params[i]) &&
@@ -571,7 +571,7 @@ rts_status rts_server_submit(rts_server *s, const rts_pair *pair, const rts_para
     std::lock_guard<std::recursive_mutex> lk(s->ctx->mu);
     rts_ctx *c = s->ctx;
     RTS_TRY(validate_params(c, *params, pair->height, pair->width));
-    if (params->aggr != RTS_AGGR_CROSS || !cross_fused_supported(*params) || !fast_costs(*params))
+    if (params->aggr != RTS_AGGR_CROSS || !cross_fused_supported(*params) || !cross_record_costs(*params))
         return set_error(c, RTS_ERR_INVALID_ARG, "the serving loop runs the fused cross-based pipeline");
     if (!s->have_params) {
         s->base_params = *params;

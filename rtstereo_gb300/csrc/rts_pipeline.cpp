@@ -296,7 +296,7 @@ rts_status run_view(rts_ctx *c, const rts_params &p, int H, int W, const ViewIn 
 static rts_status pipeline_cross_views(rts_ctx *c, const rts_params &p, int H, int W, const uint8_t *lg,
                                        const uint8_t *rg, const uint8_t *lc, const uint8_t *rc, uint8_t *dl,
                                        uint8_t *dr, uint8_t *mask) {
-    if (fast_costs(p)) {
+    if (cross_record_costs(p)) {
         // the batched form with one pair: autotuned tiles and a captured graph per shape
         rts_pair pr{W, H, lg, rg, lc, rc, nullptr, nullptr};
         rts_out o{dl, dr, mask, nullptr};
@@ -317,7 +317,7 @@ static rts_status pipeline_cross_views(rts_ctx *c, const rts_params &p, int H, i
         link_pair(&b, 0, 1);
     }
     int has_vol = 0;
-    if (!fast_costs(p)) {
+    if (!cross_record_costs(p)) {
         // other costs: the module kernels build each view's volume first
         // (the right view from mirrored copies of the images)
         has_vol = 1;
@@ -358,7 +358,7 @@ rts_status pipeline_device(rts_ctx *c, const rts_params &p, int H, int W, const 
     const size_t np = (size_t)H * W;
     cudaStream_t s = c->stream;
     // the cross-based view kernels read gray images directly when there is no colour
-    if (!cost_out && p.aggr == RTS_AGGR_CROSS && cross_fused_supported(p) && fast_costs(p))
+    if (!cost_out && p.aggr == RTS_AGGR_CROSS && cross_fused_supported(p) && cross_record_costs(p))
         return pipeline_cross_views(c, p, H, W, lg, rg, lc && rc ? lc : nullptr, lc && rc ? rc : nullptr, dl, dr,
                                     mask);
     const bool need_lab = p.aggr == RTS_AGGR_AW;

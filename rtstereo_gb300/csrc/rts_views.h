@@ -54,6 +54,10 @@ struct CrossTune {
 // Per-view item counts (host): the layout the kernels and the planner share.
 int stage_items(int stage, const ViewDesc &v, int vert_rows);
 
+// The costs the cross-based view kernels make from per-pixel records: AD and
+// census (alone or combined), and rank differences combined with census.
+bool cross_record_costs(const rts_params &p);
+
 // Host tables the cross-based kernels read (combined cost table, reciprocals);
 // made before a graph capture so that the launches find them cached.
 rts_status cross_tables(rts_ctx *c, const rts_params &p);

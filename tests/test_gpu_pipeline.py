@@ -74,6 +74,15 @@ def test_box_fused_matches_oracle(ctx, oracle_mod, W, H, D, rad, c1, c2):
     assert_same(g, o)
 
 
+@pytest.mark.parametrize("W,H,D,rank", [(96, 40, 32, 3), (70, 33, 24, 7), (150, 21, 64, 2)])
+def test_rank_census_cross_views(ctx, oracle_mod, W, H, D, rank):
+    # rank differences combined with census, cross-based: the view kernels take the
+    # ranks from the per-pixel records
+    L, Rr = synth(W + 3 * H + rank, W, H, D, 4)
+    g, o = run_both(ctx, oracle_mod, L, Rr, disp_range=D, cost1=2, cost2=3, aggr=3, rank_rad=rank)
+    assert_same(g, o)
+
+
 def test_ncc_box(ctx, oracle_mod):
     # the reference's commented-out NCC path: NCC -> box -> WTA_NCC (seq/Main.cpp:287-289)
     L, Rr = synth(77, 96, 40, 32, 4)
