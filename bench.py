@@ -295,6 +295,13 @@ def run_serve(args, rank, world):
     wall = time.perf_counter() - t0
     srv.close()
     lat = np.array(lat)
+    # per size class (the 1920x1080 pairs carry the latency target)
+    sizes = np.array([pool[c][0].shape[1] * 10000 + pool[c][0].shape[0] for c in choice[:len(lat)]])
+    by_size = {}
+    for code in sorted(set(sizes.tolist())):
+        sel = lat[sizes == code]
+        by_size[f"{code // 10000}x{code % 10000}"] = {"n": int(sel.size), "p50": float(np.percentile(sel, 50)),
+                                                      "p99": float(np.percentile(sel, 99))}
     line = {"metric": "pairs/s", "value": n / wall, "unit": "pairs/s", "n_gpus": world, "steps": n, "warmup": 4,
             "ms_per_step": wall * 1e3 / n, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": args.precision, "data": "synthetic random-dot stereo pairs (seeded)",
@@ -302,7 +309,7 @@ def run_serve(args, rank, world):
                        "hbm_budget_gb": args.budget_gb, "max_batch": args.max_batch, "sizes": MIX_SIZES,
                        "disp": MIX_DISP},
             "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
-                           "max": float(lat.max())},
+                           "max": float(lat.max()), "by_size": by_size},
             "MDE_per_s": mde / wall}
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -523,7 +530,7 @@ def main():
     ap.add_argument("--requests", type=int, default=2000, help="serve_poisson: requests in the stream")
     ap.add_argument("--rate", type=float, default=2000.0, help="serve_poisson: Poisson arrival rate (pairs/s)")
     ap.add_argument("--budget-gb", type=float, default=40.0, help="serve_poisson: HBM admitted at once")
-    ap.add_argument("--max-batch", type=int, default=8, help="serve_poisson: pairs launched together")
+    ap.add_argument("--max-batch", type=int, default=2, help="serve_poisson: pairs launched together")
     ap.add_argument("--precision", default="f32", choices=["f32", "f16"])
     ap.add_argument("--cpu-rows", type=int, default=None,
                     help="rows per CPU strip (default 48 for the 1-thread baseline, 24 for --impl reference)")
