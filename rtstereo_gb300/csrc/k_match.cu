@@ -202,6 +202,91 @@ __global__ void k_ncc(const uint8_t *__restrict__ ref, const uint8_t *__restrict
     if (den != 0.f) cost[((size_t)y * W + x) * D + d] = __fdiv_rn(nom, den);
 }
 
+// NCC over tiles (the same arithmetic as k_ncc): block per (row y, 64 pixels,
+// 64 disparities), each thread 4 pixels x 4 disparities.  Per chunk of taps the
+// block stages, in tap (raster) order, {rv, rv*rv} of its 64 reference pixels and
+// {tv, tv} of the 127 target columns t = x - d it meets (rv = I - mean, tv likewise,
+// seq/NCCDisparity.cpp:55-62).  An entry's (nom, den) pair then takes per tap
+//   (rv*tv, (rv*rv)*tv) = packed multiply of {rv, rv*rv} by {tv, tv},
+//   den term = ((rv*rv)*tv)*tv, (nom, den) += (rv*tv, den term)   (packed add)
+// which are the reference's operations in its order.
+constexpr int kNccTX = 64, kNccTD = 64, kNccTaps = 49;
+
+__global__ void __launch_bounds__(256) k_ncc_tiled(const uint8_t *__restrict__ ref, const uint8_t *__restrict__ tar,
+                                                   const float *__restrict__ mref, const float *__restrict__ mtar,
+                                                   float *__restrict__ cost, int D, int H, int W, int hr, int wr) {
+    constexpr int NT = kNccTX + kNccTD - 1;       // target columns of a tile
+    extern __shared__ __align__(16) unsigned char nsm[];
+    float2 (*rq)[kNccTX] = reinterpret_cast<float2 (*)[kNccTX]>(nsm);                         // {rv, rv*rv}
+    float2 (*tq)[NT + 1] = reinterpret_cast<float2 (*)[NT + 1]>(nsm + sizeof(float2) * kNccTaps * kNccTX);  // {tv, tv}
+    const int tid = threadIdx.x;
+    const int px0 = 4 * (tid & 15), d0 = 4 * (tid >> 4);
+    const int y = blockIdx.y, x0 = blockIdx.x * kNccTX, dc0 = blockIdx.z * kNccTD;
+    const int tbase = x0 - dc0 - (kNccTD - 1);    // target column of u = 0 (before wrapping)
+    const int ew = 2 * wr + 1, taps = (2 * hr + 1) * ew;
+    unsigned long long acc[4][4];  // (nom, den) of pixel px0 + j, disparity d0 + i
+#pragma unroll
+    for (int j = 0; j < 4; j++)
+#pragma unroll
+        for (int i = 0; i < 4; i++) acc[j][i] = 0ull;
+    for (int k0 = 0; k0 < taps; k0 += kNccTaps) {
+        const int nk = min(kNccTaps, taps - k0);
+        __syncthreads();  // the previous chunk is consumed
+        for (int q = tid; q < nk * kNccTX; q += 256) {
+            const int k = q / kNccTX, px = q - k * kNccTX;
+            const int kk = k0 + k, dy = kk / ew - hr, dx = kk - (kk / ew) * ew - wr;
+            const int x = min(x0 + px, W - 1);
+            const float mr = mref[(size_t)y * W + x];
+            const float rv = __fsub_rn((float)ref[(size_t)wrap1(y + dy, H) * W + wrap1(x + dx, W)], mr);
+            rq[k][px] = make_float2(rv, __fmul_rn(rv, rv));
+        }
+        for (int q = tid; q < nk * NT; q += 256) {
+            const int k = q / NT, u = q - k * NT;
+            const int kk = k0 + k, dy = kk / ew - hr, dx = kk - (kk / ew) * ew - wr;
+            // t in [-W, 2W) for real entries; columns of padding entries clamped into range
+            const int t = max(min(tbase + u, W - 1), -W + 1);
+            const float mt = mtar[(size_t)y * W + wrap1(t, W)];  // seq/NCCDisparity.cpp:37-48, same columns
+            const float tv = __fsub_rn((float)tar[(size_t)wrap1(y + dy, H) * W + wrap1(wrap1(t, W) + dx, W)], mt);
+            tq[k][u] = make_float2(tv, tv);
+        }
+        __syncthreads();
+        // u index of (j, i): px0 + j - d0 - i + 63
+        const int ub = px0 - d0 + kNccTD - 4;
+#pragma unroll 1
+        for (int k = 0; k < nk; k++) {
+            unsigned long long r[4], tt[7];
+            const ulonglong2 ra = *reinterpret_cast<const ulonglong2 *>(&rq[k][px0]);
+            const ulonglong2 rb = *reinterpret_cast<const ulonglong2 *>(&rq[k][px0 + 2]);
+            r[0] = ra.x; r[1] = ra.y; r[2] = rb.x; r[3] = rb.y;
+#pragma unroll
+            for (int m = 0; m < 3; m++) {
+                const ulonglong2 v = *reinterpret_cast<const ulonglong2 *>(&tq[k][ub + 2 * m]);
+                tt[2 * m] = v.x;
+                tt[2 * m + 1] = v.y;
+            }
+            tt[6] = *reinterpret_cast<const unsigned long long *>(&tq[k][ub + 6]);
+#pragma unroll
+            for (int j = 0; j < 4; j++)
+#pragma unroll
+                for (int i = 0; i < 4; i++) {
+                    const unsigned long long pr = mul2(r[j], tt[j - i + 3]);  // (rv*tv, (rv*rv)*tv)
+                    const float dt = __fmul_rn(half2_of(pr, 1), half2_of(tt[j - i + 3], 0));
+                    acc[j][i] = add2(acc[j][i], pack2(half2_of(pr, 0), dt));
+                }
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < 4; j++)
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            const int x = x0 + px0 + j, d = dc0 + d0 + i;
+            if (x < W && d < D) {
+                const float den = __fsqrt_rn(half2_of(acc[j][i], 1));  // seq/NCCDisparity.cpp:69
+                if (den != 0.f) cost[((size_t)y * W + x) * D + d] = __fdiv_rn(half2_of(acc[j][i], 0), den);
+            }
+        }
+}
+
 __global__ void k_combine(float *__restrict__ c1, const float *__restrict__ c2, long n, const float *__restrict__ lut1,
                           const float *__restrict__ lut2, float lambda1, float lambda2) {
     for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
@@ -265,7 +350,10 @@ void launch_window_mean(cudaStream_t s, const uint8_t *img, float *mean, int H, 
 }
 void launch_ncc(cudaStream_t s, const uint8_t *ref, const uint8_t *tar, const float *mref, const float *mtar,
                 float *cost, int D, int H, int W, int hr, int wr) {
-    k_ncc<<<row_grid((long)W * D, H, 256), 256, 0, s>>>(ref, tar, mref, mtar, cost, D, H, W, hr, wr);
+    const dim3 g((W + kNccTX - 1) / kNccTX, H, (D + kNccTD - 1) / kNccTD);
+    const size_t smem = sizeof(float2) * kNccTaps * (kNccTX + kNccTX + kNccTD);
+    cudaFuncSetAttribute(k_ncc_tiled, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_ncc_tiled<<<g, 256, smem, s>>>(ref, tar, mref, mtar, cost, D, H, W, hr, wr);
 }
 void launch_combine(cudaStream_t s, float *c1, const float *c2, long n, const float *lut1, const float *lut2,
                     float lambda1, float lambda2) {
