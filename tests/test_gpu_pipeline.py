@@ -83,6 +83,22 @@ def test_rank_census_cross_views(ctx, oracle_mod, W, H, D, rank):
     assert_same(g, o)
 
 
+@pytest.mark.parametrize("W,H,D", [(19, 5, 8), (45, 12, 40), (160, 30, 136), (300, 9, 200), (80, 70, 72)])
+@pytest.mark.parametrize("gray", [True, False])
+def test_cross_views_shapes(ctx, oracle_mod, W, H, D, gray):
+    # the cross-based view kernels on disparity ranges that are not multiples of 32
+    # (and above 128: eight 32-disparity chunks per lane), tiny and tall images, with
+    # and without colour images
+    import rtstereo_gb300 as R
+    O = oracle_mod
+    L, Rr = synth(W * 5 + H + D, W, H, D, 3)
+    Lc, Rc = R.gray_to_rgb(L), R.gray_to_rgb(Rr)
+    p = R.params(disp_range=D)
+    g = ctx.pipeline(p, L, Rr) if gray else ctx.pipeline(p, L, Rr, Lc, Rc)
+    o = O.pipeline(O.params(D=D, cross_L=p.cross_arm, cross_tau=p.cross_tau), L, Rr, Lc, Rc)
+    assert_same(g, o)
+
+
 def test_ncc_box(ctx, oracle_mod):
     # the reference's commented-out NCC path: NCC -> box -> WTA_NCC (seq/Main.cpp:287-289)
     L, Rr = synth(77, 96, 40, 32, 4)
