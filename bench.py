@@ -42,6 +42,7 @@ WORKLOADS = {
     "aw_1920x1080_d128": (1920, 1080, 128, 1, 3, 2, 24, 2, 3.0, 0xC2, {}),
     "rank_census_cross_1920x1080_d128": (1920, 1080, 128, 2, 3, 3, 24, 2, 3.0, 0xC2, {"rank_rad": 3}),
     "box_1920x1080_d128": (1920, 1080, 128, 1, 3, 1, 24, 2, 3.0, 0xC2, {"box_rad": 4}),
+    "log_census_cross_1920x1080_d128": (1920, 1080, 128, 4, 3, 3, 24, 2, 3.0, 0xC2, {}),
     "ncc_box_1920x1080_d128": (1920, 1080, 128, 5, 0, 1, 24, 2, 3.0, 0xC2, {"box_rad": 4, "ncc_hrad": 3,
                                                                             "ncc_wrad": 3}),
 }
