@@ -66,6 +66,52 @@ def measured_peaks():
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "sm_max_mhz": 2070.0}, "fallback"
 
 
+# ---------------------------------------------------------------------------
+# replicas under torchrun: one process per GPU, each with its own pairs (no data
+# exchange); the job's time is the slowest rank's, its work the sum of the ranks'
+
+def dist_init(world):
+    import torch
+    import torch.distributed as dist
+    if world > 1 and not dist.is_initialized():
+        # nccl on GPUs; RTS_DIST_BACKEND=gloo runs the same host logic on CPUs
+        dist.init_process_group(os.environ.get("RTS_DIST_BACKEND", "nccl"))
+    return torch
+
+
+def _reduce(vals, world, op):
+    if world <= 1:
+        return [float(v) for v in vals]
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(v) for v in vals], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=op)
+    return [float(v) for v in t.tolist()]
+
+
+def ranks_max(vals, world):
+    import torch.distributed as dist
+    return _reduce(vals, world, dist.ReduceOp.MAX if world > 1 else None)
+
+
+def ranks_sum(vals, world):
+    import torch.distributed as dist
+    return _reduce(vals, world, dist.ReduceOp.SUM if world > 1 else None)
+
+
+def ranks_barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def ranks_done(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
 class ClockSampler:
     """nvidia-smi clock / throttle sampling during the timed region."""
 
@@ -203,6 +249,7 @@ def run_batch(args, rank, world):
     import rtstereo_gb300 as R
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(dev)
+    dist_init(world)
     prec = R.PREC_F16 if args.precision == "f16" else R.PREC_F32
     data = mixed_pairs(args.pairs, 0xC3000 + 1000 * rank)
     ctx = R.Context(dev)
@@ -226,6 +273,7 @@ def run_batch(args, rank, world):
     launches0 = ctx.kernel_launches
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    ranks_barrier(world)
     with ClockSampler(dev) as clk:
         for i in range(args.steps):
             flush.zero_()
@@ -248,6 +296,9 @@ def run_batch(args, rank, world):
     t1.record(stream)
     torch.cuda.synchronize()
     ms_plain = t0.elapsed_time(t1)
+    # whole job: every rank's pairs over the slowest rank's time
+    ms, ms_plain = ranks_max([ms, ms_plain], world)
+    mde = ranks_sum([mde], world)[0]
     line = {"metric": "MDE/s", "value": mde / (ms / 1e3), "unit": "MDE/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": args.precision, "data": "synthetic random-dot stereo pairs (seeded)",
@@ -257,6 +308,7 @@ def run_batch(args, rank, world):
             "gpu_launches": ctx.kernel_launches - launches0, "clocks": clk.summary()}
     if rank == 0:
         print(json.dumps(line), flush=True)
+    ranks_done(world)
 
 
 def run_serve(args, rank, world):
@@ -265,6 +317,7 @@ def run_serve(args, rank, world):
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     import torch
     torch.cuda.set_device(dev)
+    dist_init(world)
     prec = R.PREC_F16 if args.precision == "f16" else R.PREC_F32
     pool = mixed_pairs(32, 0xC4000)
     rng = np.random.default_rng(0xC4)
@@ -278,6 +331,7 @@ def run_serve(args, rank, world):
     for L, Rr, D in pool[:4]:
         srv.wait(srv.submit(R.params(disp_range=D, precision=prec), L, Rr)[0])
     tickets = []
+    ranks_barrier(world)
     t0 = time.perf_counter()
     i = 0
     mde = 0.0
@@ -303,17 +357,22 @@ def run_serve(args, rank, world):
         sel = lat[sizes == code]
         by_size[f"{code // 10000}x{code % 10000}"] = {"n": int(sel.size), "p50": float(np.percentile(sel, 50)),
                                                       "p99": float(np.percentile(sel, 99))}
-    line = {"metric": "pairs/s", "value": n / wall, "unit": "pairs/s", "n_gpus": world, "steps": n, "warmup": 4,
+    # whole job: every rank serves its own stream; the job's wall time is the slowest's
+    wall = ranks_max([wall], world)[0]
+    served, mde = ranks_sum([n, mde], world)
+    p99_all = ranks_max([float(np.percentile(lat, 99))], world)[0]
+    line = {"metric": "pairs/s", "value": served / wall, "unit": "pairs/s", "n_gpus": world, "steps": n, "warmup": 4,
             "ms_per_step": wall * 1e3 / n, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": args.precision, "data": "synthetic random-dot stereo pairs (seeded)",
             "config": {"workload": "serve_poisson", "requests": n, "rate_per_s": args.rate,
                        "hbm_budget_gb": args.budget_gb, "max_batch": args.max_batch, "sizes": MIX_SIZES,
                        "disp": MIX_DISP},
             "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
-                           "max": float(lat.max()), "by_size": by_size},
+                           "max": float(lat.max()), "by_size": by_size, "p99_max_over_ranks": p99_all},
             "MDE_per_s": mde / wall}
     if rank == 0:
         print(json.dumps(line), flush=True)
+    ranks_done(world)
 
 
 def run_ours(args, rank, world):
@@ -322,9 +381,7 @@ def run_ours(args, rank, world):
     import rtstereo_gb300 as R
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(dev)
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl")
+    dist_init(world)
     name = args.workload
     (W, H, D, c1, c2, ag, extra), (L, Rr, Lc, Rc, Ll, Rl) = make_inputs(name)
     prec = R.PREC_F16 if args.precision == "f16" else R.PREC_F32
@@ -361,8 +418,7 @@ def run_ours(args, rank, world):
     # timed region: per-step events, L2 flushed before each step (outside the events)
     launches0 = ctx.kernel_launches
     evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    if world > 1:
-        torch.distributed.barrier()
+    ranks_barrier(world)
     torch.cuda.synchronize()
     with ClockSampler(dev) as clk:
         t0 = time.perf_counter()
@@ -373,8 +429,7 @@ def run_ours(args, rank, world):
             evs[i][1].record(stream)
         torch.cuda.synchronize()
         wall = time.perf_counter() - t0
-    if world > 1:
-        torch.distributed.barrier()
+    ranks_barrier(world)
     launches = ctx.kernel_launches - launches0
     ms_steps = [a.elapsed_time(b) for a, b in evs]
     ms = float(np.mean(ms_steps))
@@ -388,10 +443,7 @@ def run_ours(args, rank, world):
     torch.cuda.synchronize()
     stages = ctx.stage_times()
     ctx.enable_stage_timing(False)
-    if world > 1:
-        tt = torch.tensor([ms], device=f"cuda:{dev}")
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        ms = float(tt.item())
+    ms = ranks_max([ms], world)[0]
     mde_pair = W * H * D / 1e6
     value = world * mde_pair / (ms / 1e3)
 
@@ -415,10 +467,7 @@ def run_ours(args, rank, world):
         hstep()
         e_ms.append((time.perf_counter() - t1) * 1e3)
     e2e_ms = float(np.mean(e_ms))
-    if world > 1:
-        tt = torch.tensor([e2e_ms], device=f"cuda:{dev}")
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        e2e_ms = float(tt.item())
+    e2e_ms = ranks_max([e2e_ms], world)[0]
     h2d = sum(a.numel() for a in ((hL, hR) if gray_only else (hL, hR, hLc, hRc, hLl, hRl)))
     d2h = 3 * W * H
 
@@ -436,8 +485,7 @@ def run_ours(args, rank, world):
                      "mask": float((ref[2].numpy() == ho[2].numpy()).mean())}
 
     if rank != 0:
-        if world > 1:
-            torch.distributed.destroy_process_group()
+        ranks_done(world)
         return
 
     peaks, src = measured_peaks()
@@ -464,8 +512,7 @@ def run_ours(args, rank, world):
                                 "kind": "reference" if oracle.have_reference() else "port", "sample": sample,
                                 "seconds": dt}
     print(json.dumps(line), flush=True)
-    if world > 1:
-        torch.distributed.destroy_process_group()
+    ranks_done(world)
 
 
 # DRAM bytes per cost entry of the two cross-based kernels, from one ncu capture
