@@ -24,6 +24,8 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "librtstereo_gb300.so")
+DRIVER_SRC = os.path.join(PKG, "driver", "rts_stereo.cpp")
+DRIVER = os.path.join(PKG, "rts_stereo")  # headless equivalent of the reference driver
 INCLUDE = os.path.join(os.path.dirname(PKG), "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -95,6 +97,9 @@ def build(verbose: bool = False, ptxas_info: bool = False, jobs: int | None = No
         _run(["g++", "-shared", "-o", tmp] + objs +
              ["-L", libdir, "-lcudart_static", "-ldl", "-lrt", "-lpthread"])
         os.replace(tmp, LIB)
+    if _stale(DRIVER_SRC, DRIVER, headers + [LIB]):
+        _run(["g++", "-O2", "-std=c++17", "-Wall", "-I", INCLUDE, DRIVER_SRC, "-o", DRIVER,
+              "-L", PKG, "-lrtstereo_gb300", "-Wl,-rpath,$ORIGIN"])
     if verbose:
         sys.stdout.write("".join(logs))
     return LIB
