@@ -148,6 +148,12 @@ inline void disp_refinement(unsigned char *dispIm, int *HorzOffset, int *VertOff
     RTS_COMPAT_CALL(rts_disp_refinement, dispIm, HorzOffset, VertOffset, rdim, cdim, dispRange);
 }
 
+// seq/CrossBasedAggregation.h:12 declares medianFilt(image, maskSize) without
+// the image sizes (and never defines it); this overload adds them
+inline void medianFilt(unsigned char *image, int maskSize, int rdim, int cdim, int channels = 3) {
+    RTS_COMPAT_CALL(rts_medianFilt, image, rdim, cdim, channels, maskSize);
+}
+
 // seq/AdaptiveWeightAggreagtion.h:4-10
 inline void calcProxWeight(float *proxWeight, float gamma_proximity, int maskRad) {
     RTS_COMPAT_CALL(rts_calcProxWeight, proxWeight, gamma_proximity, maskRad);

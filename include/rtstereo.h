@@ -134,6 +134,13 @@ rts_status rts_cross_stereo_aggregation(rts_ctx *, rts_mem, const float *cost_im
  * the unmodified input disparities. */
 rts_status rts_disp_refinement(rts_ctx *, rts_mem, uint8_t *dispIm, const int *HorzOffset, const int *VertOffset,
                                int rdim, int cdim, int dispRange);
+/* Median pre-filter of the cross-arm images, in place: per channel the median
+ * of the maskSize x maskSize window (odd, 3..15), border pixels replicated --
+ * the OpenCV medianBlur(img, img, 3) the OpenCL driver applies to both colour
+ * images before findCross (opencl/Main.cpp:342-343).  seq declares
+ * medianFilt(image, maskSize) without sizes and never defines it
+ * (seq/CrossBasedAggregation.h:12); channels is 1 or 3 (interleaved). */
+rts_status rts_medianFilt(rts_ctx *, rts_mem, uint8_t *image, int rdim, int cdim, int channels, int maskSize);
 /* seq/AdaptiveWeightAggregation.cpp:11-18 (host arithmetic; proxWeight follows mem) */
 rts_status rts_calcProxWeight(rts_ctx *, rts_mem, float *proxWeight, float gamma_proximity, int maskRad);
 /* seq/AdaptiveWeightAggregation.cpp:33-71; weights f32 [H][W][(2r+1)^2] */
@@ -192,6 +199,9 @@ typedef struct rts_params {
     float ad_trunc;   /* seq/Main.cpp:128: 24 (AD first cost with cross-based aggregation) */
     int right_view;   /* 1: right view as flip(L2R(flip R, flip L)) and the cross-check mask */
     int precision;    /* RTS_PREC_F32 (plain) or RTS_PREC_F16 (fp16 storage, fp32 accumulation) */
+    int median_ksize; /* 0: off; odd 3..15 (cross-based only): the arms are found on median-filtered
+                         copies of the colour images, the costs on the unfiltered ones, as the OpenCL
+                         driver does (opencl/Main.cpp:342-343, medianBlur with 3) */
 } rts_params;
 
 void rts_params_default(rts_params *p);

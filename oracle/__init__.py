@@ -46,6 +46,7 @@ _ORACLE_SIGS = {
     "orc_box_inplace": [_p, _i, _i, _i, _i],
     "orc_box": [_p, _p, _i, _i, _i, _i],
     "orc_find_cross": [_p, _p, _p, _i, _i, _i, _i],
+    "orc_median": [_p, _p, _i, _i, _i, _i],
     "orc_prefix_h": [_p, _i, _i, _i],
     "orc_cross_aggr": [_p, _p, _p, _p, _p, _p, _i, _i, _i],
     "orc_prox_weight": [_p, _f, _i],
@@ -82,6 +83,7 @@ class OrcParams(C.Structure):
         ("ad_trunc", _f),
         ("right_view", _i),
         ("box_inplace", _i),
+        ("median_ksize", _i),
     ]
 
 
@@ -224,6 +226,16 @@ def box(cost, rad, inplace=False):
         return out
     out = np.empty_like(cost)
     lib().orc_box(ptr(np.ascontiguousarray(cost)), ptr(out), H, W, D, rad)
+    return out
+
+
+def median(img, k=3):
+    """Median filter of a [H][W] or [H][W][3] u8 image (k odd, borders replicated)."""
+    img = np.ascontiguousarray(img, np.uint8)
+    H, W = img.shape[:2]
+    ch = 1 if img.ndim == 2 else img.shape[2]
+    out = np.empty_like(img)
+    lib().orc_median(ptr(img), ptr(out), H, W, ch, k)
     return out
 
 

@@ -283,6 +283,29 @@ static int arm_length(const uint8_t *rgb, long centre, long step, int room, int 
     return len;
 }
 
+/* OpenCV medianBlur (opencl/Main.cpp:342-343; OpenCV documents replicated
+ * borders for it): every channel separately, the window's values sorted by
+ * insertion and the middle one taken. */
+void orc_median(const uint8_t *img, uint8_t *out, int H, int W, int ch, int k) {
+    int r = k / 2, n = k * k;
+    uint8_t v[225];
+    for (int y = 0; y < H; y++)
+        for (int x = 0; x < W; x++)
+            for (int c = 0; c < ch; c++) {
+                int m = 0;
+                for (int dy = -r; dy <= r; dy++)
+                    for (int dx = -r; dx <= r; dx++) {
+                        int yy = y + dy < 0 ? 0 : y + dy >= H ? H - 1 : y + dy;
+                        int xx = x + dx < 0 ? 0 : x + dx >= W ? W - 1 : x + dx;
+                        uint8_t a = img[((long)yy * W + xx) * ch + c];
+                        int i = m++;
+                        while (i > 0 && v[i - 1] > a) { v[i] = v[i - 1]; i--; }
+                        v[i] = a;
+                    }
+                out[((long)y * W + x) * ch + c] = v[n / 2];
+            }
+}
+
 /* seq/CrossBasedAggregation.cpp:102-115 findCross: horz[2p]=left, horz[2p+1]=right,
  * vert[2p]=top, vert[2p+1]=bottom. */
 void orc_find_cross(const uint8_t *rgb, int *horz, int *vert, int H, int W, int arm_len, int tau) {
@@ -663,9 +686,11 @@ static int one_cost(const orc_params *p, int which, int trunc_ad, int H, int W, 
     return -1;
 }
 
+/* ra / ta: the images the cross arms are found on (the colour images, or
+ * their median-filtered copies) */
 static int one_view(const orc_params *p, int H, int W, const uint8_t *rg, const uint8_t *tg,
                     const uint8_t *rc, const uint8_t *tc, const uint8_t *rl, const uint8_t *tl,
-                    uint8_t *disp, float *cost_out) {
+                    const uint8_t *ra, const uint8_t *ta, uint8_t *disp, float *cost_out) {
     long np = (long)H * W, ne = np * p->D;
     int D = p->D, rc_ = -1;
     float *c1 = (float *)malloc(ne * sizeof(float)), *c2 = NULL, *c3 = NULL;
@@ -704,8 +729,8 @@ static int one_view(const orc_params *p, int H, int W, const uint8_t *rg, const 
         int *vr = (int *)malloc(np * 2 * sizeof(int)), *vt = (int *)malloc(np * 2 * sizeof(int));
         c3 = (float *)malloc(ne * sizeof(float));
         if (!hr || !ht || !vr || !vt || !c3) { free(hr); free(ht); free(vr); free(vt); goto out; }
-        orc_find_cross(rc, hr, vr, H, W, p->cross_L, p->cross_tau);
-        orc_find_cross(tc, ht, vt, H, W, p->cross_L, p->cross_tau);
+        orc_find_cross(ra, hr, vr, H, W, p->cross_L, p->cross_tau);
+        orc_find_cross(ta, ht, vt, H, W, p->cross_L, p->cross_tau);
         orc_prefix_h(c1, H, W, D);
         orc_cross_aggr(c1, c3, hr, ht, vr, vt, H, W, D);
         free(hr); free(ht); free(vr); free(vt);
@@ -725,13 +750,41 @@ int orc_pipeline(const orc_params *p, int H, int W,
                  const uint8_t *llab, const uint8_t *rlab,
                  uint8_t *disp_left, uint8_t *disp_right, uint8_t *mask, float *cost_out) {
     if (!p || H <= 0 || W <= 0 || p->D <= 0 || p->D > 256 || p->D > W) return -1;
-    if (one_view(p, H, W, lgray, rgray, lrgb, rrgb, llab, rlab, disp_left, cost_out)) return -1;
-    if (!p->right_view) return 0;
+    if (p->median_ksize && (p->median_ksize < 3 || p->median_ksize > 15 || !(p->median_ksize & 1))) return -1;
     long np = (long)H * W;
+    /* the OpenCL driver's cross path: arms from median-filtered colour images */
+    uint8_t *med = NULL;
+    const uint8_t *la = lrgb, *ra = rrgb;
+    if (p->median_ksize && p->aggr == 3) {
+        med = (uint8_t *)malloc(np * 12);
+        if (!med) return -1;
+        orc_median(lrgb, med, H, W, 3, p->median_ksize);
+        orc_median(rrgb, med + 3 * np, H, W, 3, p->median_ksize);
+        la = med;
+        ra = med + 3 * np;
+    }
+    if (one_view(p, H, W, lgray, rgray, lrgb, rrgb, llab, rlab, la, ra, disp_left, cost_out)) {
+        free(med);
+        return -1;
+    }
+    if (!p->right_view) {
+        free(med);
+        return 0;
+    }
     uint8_t *buf = (uint8_t *)malloc(np * 14 + np);
-    if (!buf) return -1;
+    if (!buf) {
+        free(med);
+        return -1;
+    }
     uint8_t *fg_l = buf, *fg_r = fg_l + np, *fc_l = fg_r + np, *fc_r = fc_l + 3 * np;
     uint8_t *fl_l = fc_r + 3 * np, *fl_r = fl_l + 3 * np, *fd = fl_r + 3 * np;
+    uint8_t *fa_l = fc_l, *fa_r = fc_r;
+    if (med) {
+        fa_l = med + 6 * np;
+        fa_r = med + 9 * np;
+        flip_rows(la, fa_l, H, W, 3);
+        flip_rows(ra, fa_r, H, W, 3);
+    }
     flip_rows(lgray, fg_l, H, W, 1);
     flip_rows(rgray, fg_r, H, W, 1);
     flip_rows(lrgb, fc_l, H, W, 3);
@@ -740,11 +793,12 @@ int orc_pipeline(const orc_params *p, int H, int W,
         flip_rows(llab, fl_l, H, W, 3);
         flip_rows(rlab, fl_r, H, W, 3);
     }
-    int rc = one_view(p, H, W, fg_r, fg_l, fc_r, fc_l, fl_r, fl_l, fd, NULL);
+    int rc = one_view(p, H, W, fg_r, fg_l, fc_r, fc_l, fl_r, fl_l, fa_r, fa_l, fd, NULL);
     if (rc == 0) {
         flip_rows(fd, disp_right, H, W, 1);
         orc_cross_check(disp_left, disp_right, mask, H, W);
     }
     free(buf);
+    free(med);
     return rc;
 }

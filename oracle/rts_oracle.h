@@ -38,6 +38,9 @@ void orc_combine(float *c1, const float *c2, float lambda1, float lambda2, int H
 void orc_box_inplace(float *cost, int H, int W, int D, int rad);
 void orc_box(const float *cost, float *out, int H, int W, int D, int rad);
 void orc_find_cross(const uint8_t *rgb, int *horz, int *vert, int H, int W, int arm_len, int tau);
+/* OpenCV medianBlur as opencl/Main.cpp:342-343 uses it: per channel, the middle
+ * value of the k x k window, border pixels replicated (k odd). */
+void orc_median(const uint8_t *img, uint8_t *out, int H, int W, int ch, int k);
 void orc_prefix_h(float *cost, int H, int W, int D);
 void orc_cross_aggr(const float *pre, float *out, const int *hr, const int *ht, const int *vr,
                     const int *vt, int H, int W, int D);
@@ -76,6 +79,8 @@ typedef struct {
     float ad_trunc;
     int right_view;       /* 1: also compute the right view and the cross-check mask */
     int box_inplace;      /* 1: the literal in-place box of the reference */
+    int median_ksize;     /* 0, or odd: cross arms from median-filtered colour images
+                             (opencl/Main.cpp:342-343); costs from the unfiltered ones */
 } orc_params;
 
 /* Returns 0 on success, -1 on allocation failure or bad parameters.  cost_out

@@ -264,6 +264,14 @@ class Context:
         self.call("disp_refinement", HOST, out, horz, vert, H, W, D)
         return out
 
+    def medianFilt(self, img, maskSize=3):
+        """Median pre-filter of an arm image ([H][W] or [H][W][3]); returns a copy."""
+        H, W = img.shape[:2]
+        ch = 1 if img.ndim == 2 else img.shape[2]
+        out = np.array(img, np.uint8, copy=True)
+        self.call("medianFilt", HOST, out, H, W, ch, maskSize)
+        return out
+
     def calcProxWeight(self, gamma_proximity, maskRad):
         out = np.empty(((2 * maskRad + 1) ** 2,), np.float32)
         self.call("calcProxWeight", HOST, out, C.c_float(gamma_proximity), maskRad)

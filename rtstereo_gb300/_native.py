@@ -27,7 +27,8 @@ class Params(C.Structure):
     _fields_ = [("cost1", i), ("cost2", i), ("aggr", i), ("lambda1", f), ("lambda2", f), ("disp_range", i),
                 ("census_hrad", i), ("census_wrad", i), ("rank_rad", i), ("ncc_hrad", i), ("ncc_wrad", i),
                 ("box_rad", i), ("aw_rad", i), ("aw_gamma_s", f), ("aw_gamma_p", f), ("cross_arm", i),
-                ("cross_tau", i), ("ad_trunc", f), ("right_view", i), ("precision", i)]
+                ("cross_tau", i), ("ad_trunc", f), ("right_view", i), ("precision", i),
+                ("median_ksize", i)]
 
 
 class Pair(C.Structure):
@@ -87,6 +88,7 @@ SIGNATURES = {
     "rts_aggregate_cost_horizontal": (i, [p, i, p, i, i, i]),
     "rts_cross_stereo_aggregation": (i, [p, i, p, p, p, p, p, p, i, i, i]),
     "rts_disp_refinement": (i, [p, i, p, p, p, i, i, i]),
+    "rts_medianFilt": (i, [p, i, p, i, i, i, i]),
     "rts_calcProxWeight": (i, [p, i, p, f, i]),
     "rts_computeWeights": (i, [p, i, p, p, p, f, i, i, i]),
     "rts_calcAWCostL2R": (i, [p, i, p, p, p, p, i, i, i, i]),

@@ -302,6 +302,55 @@ __global__ void k_disp_refine(const uint8_t *__restrict__ in, uint8_t *__restric
 }
 
 // ---------------------------------------------------------------------------
+// Median pre-filter of the arm images: OpenCV's medianBlur, which the OpenCL
+// driver applies to both colour images before findCross
+// (opencl/Main.cpp:342-343) -- per channel, the middle value of the k x k
+// window, border pixels replicated.  The channels of a pixel are the bytes of
+// one word.  Each byte lane's median is found bit by bit from the top: a
+// candidate bit stays when at most n/2 of the n window values lie below the
+// candidate, so the result is the (n/2)-th smallest value of every lane
+// (counts stay below 256 for n <= 225).
+constexpr int kMedTX = 32, kMedTY = 8;
+
+template <int CH>
+__global__ void __launch_bounds__(kMedTX *kMedTY)
+    k_median(const uint8_t *__restrict__ in, uint8_t *__restrict__ out, int H, int W, int r) {
+    extern __shared__ uint32_t mtile[];
+    const int tw = kMedTX + 2 * r, th = kMedTY + 2 * r;
+    const int x0 = blockIdx.x * kMedTX, y0 = blockIdx.y * kMedTY;
+    for (int q = threadIdx.y * kMedTX + threadIdx.x; q < tw * th; q += kMedTX * kMedTY) {
+        const int ty = q / tw, tx = q - ty * tw;
+        const int yy = imin(imax(y0 - r + ty, 0), H - 1), xx = imin(imax(x0 - r + tx, 0), W - 1);
+        const size_t p = (size_t)yy * W + xx;
+        mtile[q] = CH == 3 ? (uint32_t)in[3 * p] | ((uint32_t)in[3 * p + 1] << 8) | ((uint32_t)in[3 * p + 2] << 16)
+                           : (uint32_t)in[p];
+    }
+    __syncthreads();
+    const int x = x0 + threadIdx.x, y = y0 + threadIdx.y;
+    if (x >= W || y >= H) return;
+    const int k = 2 * r + 1;
+    const uint32_t half = (uint32_t)(k * k / 2) * 0x01010101u;
+    uint32_t m = 0;
+    for (int bit = 7; bit >= 0; bit--) {
+        const uint32_t b = 0x01010101u << bit, cand = m | b;
+        uint32_t cnt = 0;
+        for (int dy = 0; dy < k; dy++) {
+            const uint32_t *row = mtile + (threadIdx.y + dy) * tw + threadIdx.x;
+            for (int dx = 0; dx < k; dx++) cnt += __vcmpltu4(row[dx], cand) & 0x01010101u;
+        }
+        m |= __vcmpleu4(cnt, half) & b;
+    }
+    const size_t p = (size_t)y * W + x;
+    if (CH == 3) {
+        out[3 * p] = (uint8_t)m;
+        out[3 * p + 1] = (uint8_t)(m >> 8);
+        out[3 * p + 2] = (uint8_t)(m >> 16);
+    } else {
+        out[p] = (uint8_t)m;
+    }
+}
+
+// ---------------------------------------------------------------------------
 static dim3 row_grid(long per_row, int H, int threads) { return dim3((unsigned)((per_row + threads - 1) / threads), H); }
 
 void launch_box(cudaStream_t s, const float *in, float *out, int H, int W, int D, int r) {
@@ -338,6 +387,13 @@ void launch_box_best(cudaStream_t s, const float *vol, unsigned long long *best,
 }
 void launch_find_cross(cudaStream_t s, const uint8_t *rgb, int *horz, int *vert, int H, int W, int L, int tau) {
     k_find_cross<<<row_grid(W, H, 128), 128, 0, s>>>(rgb, horz, vert, H, W, L, tau);
+}
+void launch_median(cudaStream_t s, const uint8_t *in, uint8_t *out, int H, int W, int ch, int k) {
+    const int r = k / 2;
+    const dim3 g((W + kMedTX - 1) / kMedTX, (H + kMedTY - 1) / kMedTY), b(kMedTX, kMedTY);
+    const size_t smem = (size_t)(kMedTX + 2 * r) * (kMedTY + 2 * r) * 4;
+    if (ch == 3) k_median<3><<<g, b, smem, s>>>(in, out, H, W, r);
+    else k_median<1><<<g, b, smem, s>>>(in, out, H, W, r);
 }
 void launch_prefix_h(cudaStream_t s, float *cost, int H, int W, int D) {
     const long n = (long)H * D;

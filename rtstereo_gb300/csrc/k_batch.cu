@@ -54,13 +54,24 @@ static size_t prep_smem(int gr, int gc, int L) {
     return (size_t)4 * (kPrepTW + 2 * L) * (kPrepTH + 2 * L) + (size_t)(kPrepTH + 2 * gr) * (kPrepTW + 2 * gc);
 }
 
+// the colour word of pixel p: RGB bytes, or the gray byte (replicated unless
+// the records hold gray alone)
+template <int GRAYREC>
+__device__ __forceinline__ uint32_t pixel_word(const uint8_t *img, bool rgb, size_t p) {
+    if (!rgb) return GRAYREC ? (uint32_t)img[p] : (uint32_t)img[p] * 0x010101u;
+    const uint8_t *px = img + 3 * p;
+    return (uint32_t)px[0] | ((uint32_t)px[1] << 8) | ((uint32_t)px[2] << 16);
+}
+
 // GRAYREC: the record colour is the gray byte (all views of the launch are
 // gray; the cost kernel then takes 3|dI| as the colour AD), else packed RGB with
 // gray replicated into the three channels (seq/Main.cpp:87-90).  rank >= 0: the
 // record's colour word holds the rank of the pixel instead (radius rank,
 // seq/RankFilter.cpp:11-35), which a mirrored view reads unchanged (the window
 // and its wrap are mirror symmetric).  The gray tile has a wrapped border of
-// gr rows and gc columns (the larger of the census and rank windows).
+// gr rows and gc columns (the larger of the census and rank windows).  With
+// median-filtered arm images (mref / mtar) the colour tile, and so the arms,
+// come from those, and the records from the unfiltered sources.
 template <int GRAYREC>
 __global__ void __launch_bounds__(kPrepT) k_prep_views(ViewTable t, int hr, int wr, int L, int tau, int want_code,
                                                        int rank, int gr, int gc) {
@@ -83,6 +94,8 @@ __global__ void __launch_bounds__(kPrepT) k_prep_views(ViewTable t, int hr, int 
         const int x0 = (tl - by * ntx) * kPrepTW, y0 = by * kPrepTH;
         const uint8_t *gray = img ? V.gtar : V.gref;
         const uint8_t *rgb = img ? V.ctar : V.cref;
+        // the arms may come from median-filtered copies; the records keep the source colour
+        const uint8_t *med = img ? V.mtar : V.mref;
         uint4 *rec = img ? V.rtar : V.rref;
         uint2 *arm = img ? V.atar : V.aref;
         __syncthreads();  // previous item done with the tiles
@@ -91,14 +104,7 @@ __global__ void __launch_bounds__(kPrepT) k_prep_views(ViewTable t, int hr, int 
             const int yy = y0 - L + r, xx = x0 - L + cx;
             uint32_t col = kNoPixel;
             if (yy >= 0 && yy < H && xx >= 0 && xx < W) {
-                const size_t p = (size_t)yy * W + xx;
-                if (!rgb) {
-                    col = gray[p];
-                    if (!GRAYREC) col *= 0x010101u;
-                } else {
-                    const uint8_t *px = rgb + 3 * p;
-                    col = (uint32_t)px[0] | ((uint32_t)px[1] << 8) | ((uint32_t)px[2] << 16);
-                }
+                col = pixel_word<GRAYREC>(med ? med : (rgb ? rgb : gray), rgb != nullptr, (size_t)yy * W + xx);
             }
             ct[q] = col;
         }
@@ -154,7 +160,7 @@ __global__ void __launch_bounds__(kPrepT) k_prep_views(ViewTable t, int hr, int 
             const uint32_t lr = (uint32_t)len[0] | ((uint32_t)len[1] << 16);
             const uint32_t tb = (uint32_t)len[2] | ((uint32_t)len[3] << 16);
             const size_t p = (size_t)y * W + x;
-            uint32_t cword = centre;
+            uint32_t cword = med ? pixel_word<GRAYREC>(rgb ? rgb : gray, rgb != nullptr, p) : centre;
             if (rank >= 0) {
                 // seq/RankFilter.cpp:16-29: 1 + neighbours strictly below the centre, as u8
                 const uint8_t *g0 = gt + (py + gr - rank) * gw + px + gc - rank;

@@ -75,13 +75,17 @@ GraphCache *cache_of(rts_ctx *c) {
     return (GraphCache *)c->graph_cache;
 }
 
-// Fills image/output pointers of the 2n views of n pairs.
-void fill_views(ViewBatch &b, int n, const rts_pair *pairs, const rts_out *outs, int right) {
+// Fills image/output pointers of the 2n views of n pairs; med (or nullptr)
+// holds the median-filtered arm images, left and right of every pair.
+void fill_views(ViewBatch &b, int n, const rts_pair *pairs, const rts_out *outs, int right,
+                const std::vector<uint8_t *> *med) {
     for (int i = 0; i < n; i++) {
         const rts_pair &q = pairs[i];
         ViewDesc &l = b.views[right ? 2 * i : i];
         l.gref = q.left_gray; l.gtar = q.right_gray; l.cref = q.left_rgb; l.ctar = q.right_rgb;
         if (!q.left_rgb || !q.right_rgb) l.cref = l.ctar = nullptr;
+        l.mref = med ? (*med)[2 * i] : nullptr;
+        l.mtar = med ? (*med)[2 * i + 1] : nullptr;
         l.mirror = 0;
         l.disp = outs[i].disp_left;
         l.vol = nullptr;
@@ -95,6 +99,30 @@ void fill_views(ViewBatch &b, int n, const rts_pair *pairs, const rts_out *outs,
             link_pair(&b, 2 * i, 2 * i + 1);
         }
     }
+}
+
+// Bytes of the median-filtered arm images of one pair (both images, the
+// channels of its colour images, else one).
+size_t median_pair_bytes(const rts_pair &q) {
+    const size_t np = (size_t)q.width * q.height;
+    return (np * (q.left_rgb && q.right_rgb ? 3 : 1) * 2 + 255) & ~size_t(255);
+}
+
+// Median-filters the arm images of n pairs into dst[0..n) (median_pair_bytes
+// each) on the context's stream; med receives the 2n image pointers.
+void median_pairs(rts_ctx *c, int k, int n, const rts_pair *pairs, uint8_t *const *dst, std::vector<uint8_t *> &med) {
+    StageScope sc(c, "median");
+    med.resize(2 * (size_t)n);
+    for (int i = 0; i < n; i++) {
+        const rts_pair &q = pairs[i];
+        const bool rgb = q.left_rgb && q.right_rgb;
+        const size_t bytes = (size_t)q.width * q.height * (rgb ? 3 : 1);
+        med[2 * i] = dst[i];
+        med[2 * i + 1] = dst[i] + bytes;
+        launch_median(c->stream, rgb ? q.left_rgb : q.left_gray, med[2 * i], q.height, q.width, rgb ? 3 : 1, k);
+        launch_median(c->stream, rgb ? q.right_rgb : q.right_gray, med[2 * i + 1], q.height, q.width, rgb ? 3 : 1, k);
+    }
+    count_launch(c, 2 * n);
 }
 
 void view_dims(int n, const rts_pair *pairs, const rts_params *params, int right, std::vector<int> &W,
@@ -171,9 +199,24 @@ rts_status rts::batch_views_run(rts_ctx *c, int n, const rts_pair *pairs, const 
     int gray = 1;  // records hold the gray byte as colour only when no pair has colour images
     for (int i = 0; i < n; i++)
         if (pairs[i].left_rgb && pairs[i].right_rgb) gray = 0;
+    // arms on median-filtered images: filtered ahead of the stage launches (and of the graph)
+    std::vector<uint8_t *> med;
+    if (p.median_ksize) {
+        std::vector<uint8_t *> dst(n);
+        size_t mb = 0;
+        for (int i = 0; i < n; i++) mb += median_pair_bytes(pairs[i]);
+        void *mv;
+        RTS_TRY(scratch(c, SL_V_MED, mb, &mv));
+        mb = 0;
+        for (int i = 0; i < n; i++) {
+            dst[i] = (uint8_t *)mv + mb;
+            mb += median_pair_bytes(pairs[i]);
+        }
+        median_pairs(c, p.median_ksize, n, pairs, dst.data(), med);
+    }
     ViewBatch b;
     plan_views_at(arena, W.data(), H.data(), D.data(), nv, half, &b);
-    fill_views(b, n, pairs, outs, right);
+    fill_views(b, n, pairs, outs, right, p.median_ksize ? &med : nullptr);
     // autotune once per shape: time every candidate on this batch
     auto tit = gc->tunes.find(key);
     if (tit == gc->tunes.end()) {
@@ -354,9 +397,11 @@ struct rts_server {
 
 namespace {
 
+// device bytes of a request: inputs, outputs, then its median-filtered arm images
 size_t request_device_bytes(const Request &r) {
     const size_t np = (size_t)r.pair.width * r.pair.height;
-    return ((r.in_bytes + 255) & ~size_t(255)) + ((3 * np + 255) & ~size_t(255));
+    return ((r.in_bytes + 255) & ~size_t(255)) + ((3 * np + 255) & ~size_t(255)) +
+           (r.params.median_ksize ? median_pair_bytes(r.pair) : 0);
 }
 
 void finish_batch(rts_server *s, Batch &bt) {
@@ -434,10 +479,19 @@ rts_status launch_batch(rts_server *s, std::vector<Request *> &ids) {
         if (cudaMemcpyAsync(r.d_mem, r.h_in, r.in_bytes, cudaMemcpyHostToDevice, c->stream) != cudaSuccess)
             st = set_error(c, RTS_ERR_CUDA, "server H2D copy failed");
     }
+    std::vector<uint8_t *> med;
+    if (st == RTS_OK && p.median_ksize) {
+        std::vector<uint8_t *> dst(n);
+        for (int i = 0; i < n; i++) {
+            const size_t np = (size_t)pairs[i].width * pairs[i].height;
+            dst[i] = outs[i].disp_left + ((3 * np + 255) & ~size_t(255));
+        }
+        median_pairs(c, p.median_ksize, n, pairs.data(), dst.data(), med);
+    }
     ViewBatch b;
     if (st == RTS_OK) {
         plan_views_at(bt.arena, W.data(), H.data(), D.data(), nv, half, &b);
-        fill_views(b, n, pairs.data(), outs.data(), right);
+        fill_views(b, n, pairs.data(), outs.data(), right, p.median_ksize ? &med : nullptr);
         ViewTable t;
         CrossTune tune;
         st = upload_views(c, b, tune, nullptr, &t);

@@ -32,6 +32,7 @@ enum Slot {
     SL_V_COST1, SL_V_COST2, SL_V_SEG,       // cost volumes / horizontal segment sums
     SL_V_RAW, SL_V_ROWLAST, SL_V_DISP,      // WTA winners, row summaries, view disparities
     SL_V_MEAN, SL_V_REC,                    // NCC means, fused-path pixel records
+    SL_V_MED,                               // median-filtered arm images
     SL_BATCH0, SL_BATCH1, SL_BATCH2, SL_BATCH3,
     SL_COUNT
 };
@@ -167,6 +168,9 @@ bool box_best_supported(int r);
 void launch_box_best(cudaStream_t s, const float *vol, unsigned long long *best, uint16_t *raw, int *row_last, int H,
                      int W, int D, int r, int argmax, int pos);
 void launch_find_cross(cudaStream_t s, const uint8_t *rgb, int *horz, int *vert, int H, int W, int L, int tau);
+// per-channel median of the k x k window, borders replicated (ch 1 or 3)
+inline bool median_ksize_ok(int k) { return k >= 3 && k <= 15 && (k & 1); }
+void launch_median(cudaStream_t s, const uint8_t *in, uint8_t *out, int H, int W, int ch, int k);
 void launch_prefix_h(cudaStream_t s, float *cost, int H, int W, int D);
 void launch_cross_aggr(cudaStream_t s, const float *pre, float *out, const int *hr, const int *ht, const int *vr,
                        const int *vt, int H, int W, int D);

@@ -430,6 +430,30 @@ rts_status rts_disp_refinement(rts_ctx *ctx, rts_mem m, uint8_t *disp, const int
     return finish(c, m);
 }
 
+rts_status rts_medianFilt(rts_ctx *ctx, rts_mem m, uint8_t *image, int H, int W, int ch, int k) {
+    PROLOGUE(ctx);
+    RTS_TRY(check_img(c, H, W));
+    if (!image) return bad(c, "null image");
+    if (ch != 1 && ch != 3) return bad(c, "channels must be 1 or 3");
+    if (!median_ksize_ok(k)) return bad(c, "maskSize must be odd, 3..15");
+    const size_t n = pix(H, W) * ch;
+    void *di, *tmp;
+    RTS_TRY(stage_inout(c, m, SL_IN0, image, n, &di));
+    RTS_TRY(scratch(c, SL_TMP0, n, &tmp));
+    {
+        StageScope sc(c, "median");
+        launch_median(c->stream, (const uint8_t *)di, (uint8_t *)tmp, H, W, ch, k);
+        count_launch(c);
+    }
+    RTS_TRY(check_launch(c, "median"));
+    if (m == RTS_DEVICE) {
+        RTS_CU(c, cudaMemcpyAsync(image, tmp, n, cudaMemcpyDeviceToDevice, c->stream));
+        return RTS_OK;
+    }
+    RTS_TRY(finish_out(c, m, image, tmp, n));
+    return finish(c, m);
+}
+
 rts_status rts_calcProxWeight(rts_ctx *ctx, rts_mem m, float *pw, float gamma_p, int rad) {
     PROLOGUE(ctx);
     if (!pw || rad < 0 || rad > 128) return bad(c, "bad proximity-weight arguments");

@@ -52,6 +52,8 @@ rts_status validate_params(rts_ctx *c, const rts_params &p, int H, int W) {
         return bad("adaptive-weight radius out of range");
     if (p.aggr == RTS_AGGR_CROSS && (p.cross_arm < 0 || p.cross_arm > 64)) return bad("cross arm length must be 0..64");
     if (p.cost2 != RTS_COST_NONE && (p.lambda1 == 0.f || p.lambda2 == 0.f)) return bad("lambdas must be non-zero");
+    if (p.median_ksize != 0 && (p.aggr != RTS_AGGR_CROSS || !median_ksize_ok(p.median_ksize)))
+        return bad("median_ksize must be 0, or odd in 3..15 with cross-based aggregation");
     return RTS_OK;
 }
 
@@ -221,8 +223,20 @@ static rts_status view_composed(rts_ctx *c, const rts_params &p, int H, int W, c
         RTS_TRY(scratch(c, SL_V_ARMS, np * 8 * 4, &arms));
         int *hr = (int *)arms, *vr = hr + 2 * np, *ht = vr + 2 * np, *vt = ht + 2 * np;
         RTS_TRY(scratch(c, SL_V_SEG, ne * 4, &finv));
-        launch_find_cross(s, v.cref, hr, vr, H, W, p.cross_arm, p.cross_tau);
-        launch_find_cross(s, v.ctar, ht, vt, H, W, p.cross_arm, p.cross_tau);
+        const uint8_t *ar = v.cref, *at = v.ctar;
+        if (p.median_ksize) {
+            // arms on median-filtered copies; the filter commutes with the mirroring of
+            // the right view's images (a symmetric window, replicated borders)
+            void *mv;
+            RTS_TRY(scratch(c, SL_V_MED, np * 6, &mv));
+            launch_median(s, v.cref, (uint8_t *)mv, H, W, 3, p.median_ksize);
+            launch_median(s, v.ctar, (uint8_t *)mv + 3 * np, H, W, 3, p.median_ksize);
+            count_launch(c, 2);
+            ar = (const uint8_t *)mv;
+            at = ar + 3 * np;
+        }
+        launch_find_cross(s, ar, hr, vr, H, W, p.cross_arm, p.cross_tau);
+        launch_find_cross(s, at, ht, vt, H, W, p.cross_arm, p.cross_tau);
         launch_prefix_h(s, c1, H, W, D);
         launch_cross_aggr(s, c1, (float *)finv, hr, ht, vr, vt, H, W, D);
         count_launch(c, 4);
@@ -310,6 +324,18 @@ static rts_status pipeline_cross_views(rts_ctx *c, const rts_params &p, int H, i
     RTS_TRY(plan_views(c, SL_BATCH0, Ws, Hs, Ds, nv, half, tune, &b));
     ViewDesc &v0 = b.views[0];
     v0.gref = lg; v0.gtar = rg; v0.cref = lc; v0.ctar = rc; v0.mirror = 0; v0.disp = dl;
+    if (p.median_ksize) {
+        // arms on median-filtered copies of the (three-channel) colour images
+        const size_t n3 = (size_t)H * W * 3;
+        void *mv;
+        RTS_TRY(scratch(c, SL_V_MED, n3 * 2, &mv));
+        StageScope sc(c, "median");
+        launch_median(c->stream, lc, (uint8_t *)mv, H, W, 3, p.median_ksize);
+        launch_median(c->stream, rc, (uint8_t *)mv + n3, H, W, 3, p.median_ksize);
+        count_launch(c, 2);
+        v0.mref = (const uint8_t *)mv;
+        v0.mtar = (const uint8_t *)mv + n3;
+    }
     if (nv == 2) {
         ViewDesc &v1 = b.views[1];
         v1.gref = rg; v1.gtar = lg; v1.cref = rc; v1.ctar = lc; v1.mirror = 1; v1.disp = dr;
@@ -451,6 +477,7 @@ void rts_params_default(rts_params *p) {
     p->ad_trunc = 24.f;
     p->right_view = 1;
     p->precision = RTS_PREC_F32;
+    p->median_ksize = 0;
 }
 
 rts_status rts_pipeline_run(rts_ctx *ctx, rts_mem m, const rts_pair *pair, const rts_params *params, rts_out *out) {

@@ -67,6 +67,8 @@ void link_pair(ViewBatch *b, int left, int right) {
     r.rtar = l.rref;
     r.aref = l.atar;
     r.atar = l.aref;
+    r.mref = l.mtar;
+    r.mtar = l.mref;
 }
 
 rts_status plan_views(rts_ctx *c, int slot, const int *W, const int *H, const int *D, int n, int half,

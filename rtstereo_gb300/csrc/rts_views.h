@@ -22,6 +22,7 @@ namespace rts {
 struct ViewDesc {
     const uint8_t *gref, *gtar;  // source gray images [H][W] (unmirrored)
     const uint8_t *cref, *ctar;  // source RGB images [H][W][3]
+    const uint8_t *mref, *mtar;  // median-filtered arm images (channels as cref, else as gref), or nullptr
     const float *vol;            // optional precomputed cost volume of the view [H][W][D] (or nullptr)
     int mirror;                  // 1: the view reads its sources mirrored in x
     int W, H, D;

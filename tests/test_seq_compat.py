@@ -32,6 +32,8 @@ int main() {
     calcCensusTrans(R.data(), br, 4, 3, rdim, cdim);
     calcHammingDist(bl, br, c2.data(), 4, 3, rdim, cdim, dispRange);
     combineCost(c1.data(), c2.data(), 10.0f, 10.0f, rdim, cdim, dispRange);
+    std::vector<unsigned char> Lm(Lc);  // the median pre-filter overload (result unused)
+    medianFilt(Lm.data(), 3, rdim, cdim);
     findCross(Lc.data(), hr.data(), vr.data(), rdim, cdim);
     findCross(Rc.data(), ht.data(), vt.data(), rdim, cdim);
     aggregate_cost_horizontal(c1.data(), rdim, cdim, dispRange);
