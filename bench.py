@@ -326,46 +326,56 @@ def run_serve(args, rank, world):
     choice = rng.integers(len(pool), size=n)
     ctx = R.Context(dev)
     srv = R.Server(ctx, hbm_budget=int(args.budget_gb * (1 << 30)), max_inflight=64, max_batch=args.max_batch,
-                   precision=prec)
-    # warm up the kernels on each size once
-    for L, Rr, D in pool[:4]:
+                   precision=prec, priority_pixels=args.priority_pixels)
+    # warm up: every pair of the pool once (kernels of every shape, the pinned staging)
+    for L, Rr, D in pool:
         srv.wait(srv.submit(R.params(disp_range=D, precision=prec), L, Rr)[0])
     tickets = []
     ranks_barrier(world)
     t0 = time.perf_counter()
     i = 0
     mde = 0.0
+    delay = np.zeros(n)  # arrival -> accepted by the server (host side)
     while i < n:
         now = time.perf_counter() - t0
         while i < n and arrivals[i] <= now:
             L, Rr, D = pool[choice[i]]
             tickets.append(srv.submit(R.params(disp_range=D, precision=prec), L, Rr)[0])
+            delay[i] = (time.perf_counter() - t0 - arrivals[i]) * 1e3
             mde += L.shape[0] * L.shape[1] * D / 1e6
             i += 1
         srv.progress()
-    lat = []
+    lat, queue, run = [], [], []
     for t in tickets:
         sub, start, done = srv.wait(t)
         lat.append(done - sub)
+        queue.append(start - sub)
+        run.append(done - start)
     wall = time.perf_counter() - t0
     srv.close()
-    lat = np.array(lat)
-    # per size class (the 1920x1080 pairs carry the latency target)
+    lat, queue, run = np.array(lat), np.array(queue), np.array(run)
+    # per size class (the 1920x1080 pairs carry the latency target); the parts of
+    # a request's latency: waiting for admission, then launch to completion seen
+    # by the host; and the host's delay from the request's arrival to its submit
     sizes = np.array([pool[c][0].shape[1] * 10000 + pool[c][0].shape[0] for c in choice[:len(lat)]])
     by_size = {}
     for code in sorted(set(sizes.tolist())):
-        sel = lat[sizes == code]
-        by_size[f"{code // 10000}x{code % 10000}"] = {"n": int(sel.size), "p50": float(np.percentile(sel, 50)),
-                                                      "p99": float(np.percentile(sel, 99))}
+        m = sizes == code
+        sel = lat[m]
+        by_size[f"{code // 10000}x{code % 10000}"] = {
+            "n": int(sel.size), "p50": float(np.percentile(sel, 50)), "p99": float(np.percentile(sel, 99)),
+            "queue_p99": float(np.percentile(queue[m], 99)), "run_p50": float(np.percentile(run[m], 50)),
+            "run_p99": float(np.percentile(run[m], 99)), "submit_delay_p99": float(np.percentile(delay[m], 99))}
     # whole job: every rank serves its own stream; the job's wall time is the slowest's
     wall = ranks_max([wall], world)[0]
     served, mde = ranks_sum([n, mde], world)
     p99_all = ranks_max([float(np.percentile(lat, 99))], world)[0]
-    line = {"metric": "pairs/s", "value": served / wall, "unit": "pairs/s", "n_gpus": world, "steps": n, "warmup": 4,
+    line = {"metric": "pairs/s", "value": served / wall, "unit": "pairs/s", "n_gpus": world, "steps": n, "warmup": len(pool),
             "ms_per_step": wall * 1e3 / n, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": args.precision, "data": "synthetic random-dot stereo pairs (seeded)",
             "config": {"workload": "serve_poisson", "requests": n, "rate_per_s": args.rate,
-                       "hbm_budget_gb": args.budget_gb, "max_batch": args.max_batch, "sizes": MIX_SIZES,
+                       "hbm_budget_gb": args.budget_gb, "max_batch": args.max_batch,
+                       "priority_pixels": args.priority_pixels, "sizes": MIX_SIZES,
                        "disp": MIX_DISP},
             "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
                            "max": float(lat.max()), "by_size": by_size, "p99_max_over_ranks": p99_all},
@@ -579,6 +589,9 @@ def main():
     ap.add_argument("--rate", type=float, default=2000.0, help="serve_poisson: Poisson arrival rate (pairs/s)")
     ap.add_argument("--budget-gb", type=float, default=40.0, help="serve_poisson: HBM admitted at once")
     ap.add_argument("--max-batch", type=int, default=2, help="serve_poisson: pairs launched together")
+    ap.add_argument("--priority-pixels", type=int, default=1920 * 1080,
+                    help="serve_poisson: pairs of at least this many pixels run alone on high-priority streams "
+                         "(0: one class)")
     ap.add_argument("--precision", default="f32", choices=["f32", "f16"])
     ap.add_argument("--cpu-rows", type=int, default=None,
                     help="rows per CPU strip (default 48 for the 1-thread baseline, 24 for --impl reference)")

@@ -240,6 +240,8 @@ typedef struct rts_server_config {
     int max_inflight;    /* slots: pairs on the device at once */
     int max_batch;       /* pairs launched together */
     int precision;       /* RTS_PREC_F32 or RTS_PREC_F16 */
+    long long priority_pixels; /* 0: one class; else requests of at least this many pixels
+                                  run alone on high-priority streams, the others in batches */
 } rts_server_config;
 
 typedef struct rts_request_stats {

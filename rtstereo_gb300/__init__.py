@@ -338,11 +338,11 @@ class Server:
     """rts_server: continuous-batching request loop over one context."""
 
     def __init__(self, ctx: Context, hbm_budget: int, max_inflight: int = 64, max_batch: int = 16,
-                 precision: int = PREC_F16):
+                 precision: int = PREC_F16, priority_pixels: int = 0):
         self.ctx = ctx
         self._lib = ctx._lib
         h = C.c_void_p()
-        cfg = ServerConfig(hbm_budget, max_inflight, max_batch, precision)
+        cfg = ServerConfig(hbm_budget, max_inflight, max_batch, precision, priority_pixels)
         ctx.check(self._lib.rts_server_create(C.byref(h), ctx.h, C.byref(cfg)), "server_create")
         self.h = h
         self._keep = {}

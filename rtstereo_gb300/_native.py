@@ -44,7 +44,8 @@ class Out(C.Structure):
 
 class ServerConfig(C.Structure):
     """rts_server_config"""
-    _fields_ = [("hbm_budget", sz), ("max_inflight", i), ("max_batch", i), ("precision", i)]
+    _fields_ = [("hbm_budget", sz), ("max_inflight", i), ("max_batch", i), ("precision", i),
+                ("priority_pixels", C.c_longlong)]
 
 
 class RequestStats(C.Structure):

@@ -763,7 +763,7 @@ rts_status launch_cross_views(rts_ctx *c, const rts_params &p, const ViewTable &
     const int sms = num_sms();
     auto grid = [&](int items, int per_block, int per_sm) {
         const long need = ((long)items + per_block - 1) / per_block;
-        const long cap = (long)sms * per_sm;
+        const long cap = tune.persistent ? (long)sms * per_sm : need;
         return (unsigned)(need < cap ? (need > 0 ? need : 1) : cap);
     };
     const int L = p.cross_arm;

@@ -349,6 +349,47 @@ struct Pool {
     }
 };
 
+// Pinned host staging kept across requests: pinning and unpinning pages is far
+// slower than a request's copies (and freeing pinned memory waits for the
+// device), so released blocks go to a free list by size and are handed out
+// again; beyond `cap` cached bytes a released block is freed.
+struct HostCache {
+    std::multimap<size_t, unsigned char *> free_;       // block size -> block
+    std::unordered_map<unsigned char *, size_t> size_;  // every live or cached block
+    size_t cached = 0, cap = size_t(4) << 30;
+    unsigned char *get(size_t bytes) {
+        bytes = (bytes + 65535) & ~size_t(65535);
+        auto it = free_.lower_bound(bytes);
+        if (it != free_.end() && it->first <= 2 * bytes) {
+            unsigned char *p = it->second;
+            cached -= it->first;
+            free_.erase(it);
+            return p;
+        }
+        unsigned char *p = nullptr;
+        if (cudaHostAlloc((void **)&p, bytes, cudaHostAllocDefault) != cudaSuccess) {
+            cudaGetLastError();
+            return nullptr;
+        }
+        size_[p] = bytes;
+        return p;
+    }
+    void put(unsigned char *p) {
+        if (!p) return;
+        const size_t bytes = size_[p];
+        if (cached + bytes > cap) {
+            size_.erase(p);
+            cudaFreeHost(p);
+            return;
+        }
+        free_.emplace(bytes, p);
+        cached += bytes;
+    }
+    ~HostCache() {
+        for (auto &kv : size_) cudaFreeHost(kv.first);
+    }
+};
+
 enum ReqState { RQ_PENDING, RQ_RUNNING, RQ_DONE, RQ_CANCELLED, RQ_FAILED };
 
 struct Request {
@@ -356,7 +397,8 @@ struct Request {
     rts_pair pair;
     rts_params params;
     rts_out out;               // caller's host buffers
-    unsigned char *h_in = nullptr;  // pinned copy of the inputs: gray L, gray R, (rgb L, rgb R)
+    unsigned char *h_in = nullptr;  // pinned copy of the inputs: gray L, gray R, (rgb L, rgb R);
+                                    // then, in the same staging block, h_out
     unsigned char *h_out = nullptr; // pinned outputs: disp L, disp R, mask
     size_t in_bytes = 0, out_bytes = 0;
     void *d_mem = nullptr;     // device: inputs + outputs
@@ -373,6 +415,7 @@ struct Batch {
     cudaStream_t stream = nullptr;
     cudaEvent_t done = nullptr;
     bool active = false;
+    bool high = false;  // on a high-priority stream (large requests, launched alone)
 };
 
 }  // namespace
@@ -390,6 +433,7 @@ struct rts_server {
     int next_stream = 0;
     rts_params base_params{};
     bool have_params = false;
+    HostCache staging;
     Clock::time_point t0 = Clock::now();
     std::mutex mu;
     double now_ms() const { return std::chrono::duration<double, std::milli>(Clock::now() - t0).count(); }
@@ -421,6 +465,9 @@ void finish_batch(rts_server *s, Batch &bt) {
         r.t_done = s->now_ms();
         s->pool.release(r.d_mem, r.d_bytes);
         r.d_mem = nullptr;
+        // the device is done with the staging and the result is delivered
+        s->staging.put(r.h_in);
+        r.h_in = r.h_out = nullptr;
         s->inflight--;
     }
     s->pool.release(bt.arena, bt.arena_bytes);
@@ -429,17 +476,23 @@ void finish_batch(rts_server *s, Batch &bt) {
     bt.active = false;
 }
 
-// Launches the requests in `ids` as one batch on the next free stream.
-rts_status launch_batch(rts_server *s, std::vector<Request *> &ids) {
-    rts_ctx *c = s->ctx;
-    int slot = -1;
+bool is_large(const rts_server *s, const Request &r) {
+    return s->cfg.priority_pixels > 0 && (long long)r.pair.width * r.pair.height >= s->cfg.priority_pixels;
+}
+
+// A free stream of the given class, round robin; -1 if none.
+int free_slot(const rts_server *s, bool high) {
     for (int k = 0; k < (int)s->batches.size(); k++) {
         const int j = (s->next_stream + k) % (int)s->batches.size();
-        if (!s->batches[j].active) {
-            slot = j;
-            break;
-        }
+        if (!s->batches[j].active && s->batches[j].high == high) return j;
     }
+    return -1;
+}
+
+// Launches the requests in `ids` as one batch on a free stream of their class.
+rts_status launch_batch(rts_server *s, std::vector<Request *> &ids) {
+    rts_ctx *c = s->ctx;
+    const int slot = free_slot(s, is_large(s, *ids[0]));
     if (slot < 0) return RTS_ERR_BUSY;
     Batch &bt = s->batches[slot];
     const int n = (int)ids.size();
@@ -494,6 +547,12 @@ rts_status launch_batch(rts_server *s, std::vector<Request *> &ids) {
         fill_views(b, n, pairs.data(), outs.data(), right, p.median_ksize ? &med : nullptr);
         ViewTable t;
         CrossTune tune;
+        if (s->cfg.priority_pixels > 0 && !bt.high) {
+            // one block per work item, short items: the blocks of a large request
+            // launched meanwhile on a high-priority stream take the SMs as these retire
+            tune.persistent = 0;
+            tune.vert_rows = 256;
+        }
         st = upload_views(c, b, tune, nullptr, &t);
         if (st == RTS_OK) st = launch_cross_views(c, p, t, half, 0, gray, b.max_d, tune, b.row_last_all, b.row_last_count);
     }
@@ -530,46 +589,51 @@ rts_status progress_locked(rts_server *s) {
         if (q == cudaSuccess) finish_batch(s, bt);
         else if (q != cudaErrorNotReady) return cuda_check(s->ctx, q, "server batch");
     }
-    // admission in arrival order while a stream, a slot and device memory are free
-    bool free_stream = false;
-    for (Batch &bt : s->batches) free_stream |= !bt.active;
-    if (!free_stream) return RTS_OK;
-    std::vector<Request *> batch;
-    size_t batch_bytes = 0;
-    while (!s->queue.empty() && (int)batch.size() < s->cfg.max_batch && s->inflight < s->cfg.max_inflight) {
-        Request &r = *s->reqs[s->queue.front()];
-        if (r.state == RQ_CANCELLED) {
+    // admission in arrival order while a stream of the request's class, a slot and
+    // device memory are free; a large request (priority_pixels) goes alone
+    for (;;) {
+        while (!s->queue.empty() && s->reqs[s->queue.front()]->state == RQ_CANCELLED) s->queue.pop_front();
+        if (s->queue.empty()) return RTS_OK;
+        const bool high = is_large(s, *s->reqs[s->queue.front()]);
+        if (free_slot(s, high) < 0) return RTS_OK;
+        const int max_batch = high ? 1 : s->cfg.max_batch;
+        std::vector<Request *> batch;
+        size_t batch_bytes = 0;
+        while (!s->queue.empty() && (int)batch.size() < max_batch && s->inflight < s->cfg.max_inflight) {
+            Request &r = *s->reqs[s->queue.front()];
+            if (r.state == RQ_CANCELLED) {
+                s->queue.pop_front();
+                continue;
+            }
+            if (is_large(s, r) != high) break;  // the next request is of the other class
+            // the request's own buffers plus its share of the batch scratch
+            int Wv[2] = {r.pair.width, r.pair.width}, Hv[2] = {r.pair.height, r.pair.height},
+                Dv[2] = {r.params.disp_range, r.params.disp_range};
+            const size_t need_scratch = views_bytes(Wv, Hv, Dv, r.params.right_view ? 2 : 1,
+                                                    s->base_params.precision == RTS_PREC_F16);
+            const size_t need = request_device_bytes(r);
+            if (s->pool.used + batch_bytes + need + need_scratch + 65536 > s->pool.size) break;  // wait for memory
+            r.d_bytes = need;
+            r.d_mem = s->pool.alloc(need);
+            if (!r.d_mem) break;
+            batch_bytes += need_scratch;
             s->queue.pop_front();
-            continue;
+            s->inflight++;
+            batch.push_back(&r);
         }
-        // the request's own buffers plus its share of the batch scratch
-        int Wv[2] = {r.pair.width, r.pair.width}, Hv[2] = {r.pair.height, r.pair.height},
-            Dv[2] = {r.params.disp_range, r.params.disp_range};
-        const size_t need_scratch = views_bytes(Wv, Hv, Dv, r.params.right_view ? 2 : 1,
-                                                s->base_params.precision == RTS_PREC_F16);
-        const size_t need = request_device_bytes(r);
-        if (s->pool.used + batch_bytes + need + need_scratch + 65536 > s->pool.size) break;  // wait for memory
-        r.d_bytes = need;
-        r.d_mem = s->pool.alloc(need);
-        if (!r.d_mem) break;
-        batch_bytes += need_scratch;
-        s->queue.pop_front();
-        s->inflight++;
-        batch.push_back(&r);
-    }
-    if (batch.empty()) return RTS_OK;
-    rts_status st = launch_batch(s, batch);
-    if (st != RTS_OK) {
-        // put the requests back at the head of the queue
-        for (auto it = batch.rbegin(); it != batch.rend(); ++it) {
-            s->pool.release((*it)->d_mem, (*it)->d_bytes);
-            (*it)->d_mem = nullptr;
-            s->inflight--;
-            s->queue.push_front((*it)->ticket);
+        if (batch.empty()) return RTS_OK;
+        rts_status st = launch_batch(s, batch);
+        if (st != RTS_OK) {
+            // put the requests back at the head of the queue
+            for (auto it = batch.rbegin(); it != batch.rend(); ++it) {
+                s->pool.release((*it)->d_mem, (*it)->d_bytes);
+                (*it)->d_mem = nullptr;
+                s->inflight--;
+                s->queue.push_front((*it)->ticket);
+            }
+            return st == RTS_ERR_BUSY ? RTS_OK : st;
         }
-        return st == RTS_ERR_BUSY ? RTS_OK : st;
     }
-    return RTS_OK;
 }
 
 }  // namespace
@@ -588,11 +652,20 @@ rts_status rts_server_create(rts_server **out, rts_ctx *ctx, const rts_server_co
         delete s;
         return set_error(ctx, RTS_ERR_OOM, "cannot reserve the server's device pool");
     }
-    const int nstreams = 3;
-    s->streams.resize(nstreams);
-    s->batches.resize(nstreams);
-    for (int i = 0; i < nstreams; i++) {
-        if (cudaStreamCreateWithFlags(&s->streams[i], cudaStreamNonBlocking) != cudaSuccess ||
+    // three streams at the default priority; with priority_pixels, two more at the
+    // greatest priority for the large requests (their blocks are dispatched first)
+    const int nlow = 3, nhigh = cfg->priority_pixels > 0 ? 2 : 0;
+    int least = 0, greatest = 0;
+    if (cudaDeviceGetStreamPriorityRange(&least, &greatest) != cudaSuccess) {
+        delete s;
+        return RTS_ERR_CUDA;
+    }
+    s->streams.resize(nlow + nhigh);
+    s->batches.resize(nlow + nhigh);
+    for (int i = 0; i < nlow + nhigh; i++) {
+        s->batches[i].high = i >= nlow;
+        if (cudaStreamCreateWithPriority(&s->streams[i], cudaStreamNonBlocking, i >= nlow ? greatest : least) !=
+                cudaSuccess ||
             cudaEventCreateWithFlags(&s->batches[i].done, cudaEventDisableTiming) != cudaSuccess) {
             rts_server_destroy(s);
             return RTS_ERR_CUDA;
@@ -607,10 +680,6 @@ void rts_server_destroy(rts_server *s) {
     cudaSetDevice(s->ctx->device);
     for (auto st : s->streams)
         if (st) cudaStreamSynchronize(st);
-    for (auto &kv : s->reqs) {
-        if (kv.second->h_in) cudaFreeHost(kv.second->h_in);
-        if (kv.second->h_out) cudaFreeHost(kv.second->h_out);
-    }
     for (auto &b : s->batches)
         if (b.done) cudaEventDestroy(b.done);
     for (auto st : s->streams)
@@ -652,11 +721,9 @@ rts_status rts_server_submit(rts_server *s, const rts_pair *pair, const rts_para
     if (request_device_bytes(*r) + views_bytes(Wv, Hv, Dv, params->right_view ? 2 : 1,
                                                params->precision == RTS_PREC_F16) > s->pool.size)
         return set_error(c, RTS_ERR_BUSY, "request larger than the server's HBM budget");
-    if (cudaHostAlloc((void **)&r->h_in, r->in_bytes, cudaHostAllocDefault) != cudaSuccess ||
-        cudaHostAlloc((void **)&r->h_out, r->out_bytes, cudaHostAllocDefault) != cudaSuccess) {
-        if (r->h_in) cudaFreeHost(r->h_in);
-        return set_error(c, RTS_ERR_OOM, "pinned host memory");
-    }
+    r->h_in = s->staging.get(((r->in_bytes + 255) & ~size_t(255)) + r->out_bytes);
+    if (!r->h_in) return set_error(c, RTS_ERR_OOM, "pinned host memory");
+    r->h_out = r->h_in + ((r->in_bytes + 255) & ~size_t(255));
     memcpy(r->h_in, pair->left_gray, np);
     memcpy(r->h_in + np, pair->right_gray, np);
     if (rgb) {
@@ -701,11 +768,8 @@ rts_status rts_server_wait(rts_server *s, uint64_t ticket, double timeout_ms, rt
         if (r == -(int)RTS_ERR_CANCELLED) {
             std::lock_guard<std::mutex> g(s->mu);
             auto it = s->reqs.find(ticket);
-            if (it != s->reqs.end() && it->second->d_mem == nullptr) {  // no longer on the device
-                cudaFreeHost(it->second->h_in);
-                cudaFreeHost(it->second->h_out);
+            if (it != s->reqs.end() && it->second->d_mem == nullptr)  // no longer on the device
                 s->reqs.erase(it);
-            }
             return RTS_ERR_CANCELLED;
         }
         if (r < 0) return (rts_status)(-r);
@@ -716,9 +780,6 @@ rts_status rts_server_wait(rts_server *s, uint64_t ticket, double timeout_ms, rt
     auto it = s->reqs.find(ticket);
     Request &r = *it->second;
     if (stats) *stats = rts_request_stats{r.t_submit, r.t_start, r.t_done};
-    // the result has been delivered: the request's host staging can go
-    cudaFreeHost(r.h_in);
-    cudaFreeHost(r.h_out);
     s->reqs.erase(it);
     return RTS_OK;
 }
@@ -731,6 +792,8 @@ rts_status rts_server_cancel(rts_server *s, uint64_t ticket) {
     Request &r = *it->second;
     if (r.state == RQ_PENDING) {
         r.state = RQ_CANCELLED;  // skipped at admission
+        s->staging.put(r.h_in);
+        r.h_in = r.h_out = nullptr;
         return RTS_OK;
     }
     if (r.state == RQ_RUNNING) {

@@ -50,6 +50,7 @@ struct ViewTable {
 struct CrossTune {
     int vert_rows = 4096;   // output rows per vertical-aggregation item (a strip of one column)
     int grid_mult = 8;      // persistent blocks per SM of the row-segment kernel
+    int persistent = 1;     // 0: one block per work item (no cap at the resident blocks)
 };
 
 // Per-view item counts (host): the layout the kernels and the planner share.

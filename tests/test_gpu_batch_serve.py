@@ -64,9 +64,13 @@ def test_batch_matches_single_runs(ctx, oracle_mod, prec):
         assert all(bits_equal(a, b) for a, b in zip(g, o[:3]))
 
 
-def test_server_same_alone_and_in_the_mix(ctx):
+@pytest.mark.parametrize("priority_pixels", [0, 128 * 128])
+def test_server_same_alone_and_in_the_mix(ctx, priority_pixels):
+    """With priority_pixels the larger pairs of the mix run alone on high-priority
+    streams while the smaller ones are batched; results do not change."""
     import rtstereo_gb300 as R
-    srv = R.Server(ctx, hbm_budget=1 << 30, max_inflight=8, max_batch=3, precision=R.PREC_F16)
+    srv = R.Server(ctx, hbm_budget=1 << 30, max_inflight=8, max_batch=3, precision=R.PREC_F16,
+                   priority_pixels=priority_pixels)
     try:
         data = make_pairs(55) * 3
         tickets = []
