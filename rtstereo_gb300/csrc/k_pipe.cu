@@ -364,6 +364,272 @@ __global__ void __launch_bounds__(kAwThreads, 3) k_aw_wta(const CT *__restrict__
 }
 
 // ---------------------------------------------------------------------------
+// The plain form of k_aw_wta, software-pipelined over the tap rows: while the
+// block adds tap row ky, the cost rows of ky + 1 arrive by cp.async in the
+// other buffer, the weights of ky + 1 are made in slices between the groups of
+// taps (their table reads in flight across a group), and the Lab rows of
+// ky + 2 are staged; one barrier per tap row.  The arithmetic per entry is
+// k_aw_wta's (the reference's order, unfused), so the results are the same.
+template <int DUMMY>
+__global__ void __launch_bounds__(kAwThreads, 2) k_aw_wta_pipe(const float *__restrict__ vol,
+                                                          const uint32_t *__restrict__ labr,
+                                                          const uint32_t *__restrict__ labt,
+                                                          const float *__restrict__ pw, const float *__restrict__ G,
+                                                          uint16_t *__restrict__ raw, int *__restrict__ row_last,
+                                                          float *__restrict__ cost_out, int H, int W, int D, int e) {
+    const int r = e >> 1;
+    constexpr int NT = kAwTX + kAwDC - 1;  // target columns of a tile
+    constexpr int NTP = NT + 1;
+    const int CS = (kAwTX + 2 * r + 4) * kAwCPitch;  // floats of one cost buffer
+    extern __shared__ __align__(16) float asm_[];
+    // buffer b: costs at asm_ + b CS, reference weights at wR0 + b e 64, target weights at wT0 + b e NTP
+    float *const wR0 = asm_ + 2 * CS, *const wT0 = wR0 + 2 * e * kAwTX;
+    uint32_t *labbase = reinterpret_cast<uint32_t *>(asm_ + 2 * CS + 2 * e * kAwTX + 2 * e * NTP);
+    const int LRN = kAwTX + 2 * r, LTN = NT + 2 * r;  // words of a reference / target Lab row
+    __shared__ float best_v[kAwTX];
+    __shared__ int best_i[kAwTX];
+
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    constexpr int NW = kAwThreads / 32;
+    const int td = lane & 15;
+    const int px0 = 8 * warp + 4 * (lane >> 4);
+    const int y = blockIdx.y, x0 = blockIdx.x * kAwTX;
+    if (tid < kAwTX) {
+        best_v[tid] = __int_as_float(0x7f800000);
+        best_i[tid] = 0x7fffffff;
+    }
+    const bool vec = (D & 3) == 0;
+
+    for (int dc0 = 0; dc0 < D; dc0 += kAwDC) {
+        unsigned long long sw[4][2], sc[4][2];
+#pragma unroll
+        for (int j = 0; j < 4; j++)
+#pragma unroll
+            for (int h = 0; h < 2; h++) sw[j][h] = sc[j][h] = 0ull;
+        const int tbase = x0 - dc0 - (kAwDC - 1);
+        uint32_t cR[2], cT[4];
+#pragma unroll
+        for (int m = 0; m < 2; m++) {
+            const int x = x0 + lane + 32 * m;
+            cR[m] = x < W ? labr[(size_t)y * W + x] : kLabOut;
+        }
+#pragma unroll
+        for (int m = 0; m < 4; m++) {
+            int t = tbase + lane + 32 * m;
+            if (t < 0) t += W;  // seq/AdaptiveWeightAggregation.cpp:87
+            cT[m] = (lane + 32 * m < NT && t >= 0 && t < W) ? labt[(size_t)y * W + t] : kLabOut;
+        }
+        const bool wrapped_tile = tbase < 0;
+        const int ky_lo = imax(-r, -y), ky_hi = imin(r, H - 1 - y);
+
+        // cost rows of tap row ky into C by cp.async (zero fill past D); wrapped
+        // columns as in k_aw_wta (seq/AdaptiveWeightAggregation.cpp:95-97)
+        auto stage_cost = [&](int ky, float *C) {
+            const size_t crow = (size_t)(y + ky) * W;
+            const uint32_t cbase = (uint32_t)__cvta_generic_to_shared(C);
+            if (vec) {
+                for (int q = tid; q < (kAwTX + 2 * r) * (kAwDC / 4); q += kAwThreads) {
+                    const int xi = q >> 4, d4 = (q & 15) * 4;
+                    const int xs = imin(imax(wrap1(x0 - r + xi, W), 0), W - 1);
+                    const int dg = dc0 + d4;
+                    const float *src = vol + (crow + xs) * D + (dg < D ? dg : 0);
+                    const uint32_t dst = cbase + (uint32_t)((xi * kAwCPitch + d4) * 4);
+                    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(dst), "l"(src),
+                                 "r"(dg < D ? 16 : 0)
+                                 : "memory");
+                }
+            } else {
+                for (int q = tid; q < (kAwTX + 2 * r) * kAwDC; q += kAwThreads) {
+                    const int xi = q >> 6, dd = q & 63;
+                    const int xs = imin(imax(wrap1(x0 - r + xi, W), 0), W - 1);
+                    const int dg = dc0 + dd;
+                    const float *src = vol + (crow + xs) * D + (dg < D ? dg : 0);
+                    const uint32_t dst = cbase + (uint32_t)((xi * kAwCPitch + dd) * 4);
+                    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(dst), "l"(src),
+                                 "r"(dg < D ? 4 : 0)
+                                 : "memory");
+                }
+            }
+            asm volatile("cp.async.commit_group;\n" ::: "memory");
+        };
+        auto stage_lab = [&](int ky, int slot) {
+            const size_t crow = (size_t)(y + ky) * W;
+            uint32_t *LR = labbase + slot * (LRN + LTN), *LT = LR + LRN;
+            for (int q = tid; q < LRN; q += kAwThreads) {
+                const int xc = x0 - r + q;
+                LR[q] = (xc >= 0 && xc < W) ? labr[crow + xc] : kLabOut;
+            }
+            for (int q = tid; q < LTN; q += kAwThreads) {
+                const int xc = tbase - r + q;
+                LT[q] = (xc >= 0 && xc < W) ? labt[crow + xc] : kLabOut;
+            }
+        };
+        // weights of tap (ky, k) for this warp's lanes, in two halves: the table
+        // indices and reads (issue), then the products (finish)
+        struct Slice {
+            uint32_t idx[6];
+            bool ok[6];
+            float g[6];
+        };
+        auto slice_issue = [&](Slice &sl, int ky, int k, int slot) {
+            const uint32_t *LR = labbase + slot * (LRN + LTN), *LT = LR + LRN;
+            const size_t crow = (size_t)(y + ky) * W;
+#pragma unroll
+            for (int m = 0; m < 2; m++) {
+                const uint32_t q = LR[imin(lane + 32 * m + k, LRN - 1)];
+                sl.ok[m] = k < e && !((q | cR[m]) & kLabOut);
+                const uint32_t ad = __vabsdiffu4(cR[m], q);
+                sl.idx[m] = __dp4a(ad, ad, 0u);
+            }
+#pragma unroll
+            for (int m = 0; m < 4; m++) {
+                const int u = lane + 32 * m;
+                uint32_t q = LT[imin(u + k, LTN - 1)];
+                if (wrapped_tile && tbase + u < 0 && k < e) {
+                    const int xc = tbase + u + W + k - r;
+                    q = (xc >= 0 && xc < W) ? labt[crow + xc] : kLabOut;
+                }
+                sl.ok[2 + m] = k < e && u < NT && !((q | cT[m]) & kLabOut);
+                const uint32_t ad = __vabsdiffu4(cT[m], q);
+                sl.idx[2 + m] = __dp4a(ad, ad, 0u);
+            }
+#pragma unroll
+            for (int m = 0; m < 6; m++) sl.g[m] = sl.ok[m] ? __ldg(G + sl.idx[m]) : 0.f;
+        };
+        auto slice_finish = [&](const Slice &sl, int ky, int k, float *wR, float *wT) {
+            if (k < e) {
+                // seq/AdaptiveWeightAggregation.cpp:33-71: pw[k] * expf(-dist / gamma_s)
+                const float pwk = __ldg(pw + (ky + r) * e + k);
+#pragma unroll
+                for (int m = 0; m < 2; m++) wR[k * kAwTX + lane + 32 * m] = sl.ok[m] ? __fmul_rn(pwk, sl.g[m]) : 0.f;
+#pragma unroll
+                for (int m = 0; m < 4; m++) {
+                    const int u = lane + 32 * m;
+                    if (u < NT) wT[k * NTP + u] = sl.ok[2 + m] ? __fmul_rn(pwk, sl.g[2 + m]) : 0.f;
+                }
+            }
+        };
+
+        // prologue: Lab rows of the first two tap rows, costs and weights of the first
+        __syncthreads();  // the previous chunk is done with every buffer
+        stage_lab(ky_lo, 0);
+        if (ky_lo + 1 <= ky_hi) stage_lab(ky_lo + 1, 1);
+        stage_cost(ky_lo, asm_);
+        __syncthreads();
+        for (int k = warp; k < e; k += NW) {
+            Slice sl;
+            slice_issue(sl, ky_lo, k, 0);
+            slice_finish(sl, ky_lo, k, wR0, wT0);
+        }
+        asm volatile("cp.async.wait_all;\n" ::: "memory");
+        __syncthreads();
+
+        for (int ky = ky_lo; ky <= ky_hi; ky++) {
+            const int i = ky - ky_lo, b = i & 1;
+            const bool next = ky + 1 <= ky_hi;
+            if (next) stage_cost(ky + 1, asm_ + (b ^ 1) * CS);
+            if (ky + 2 <= ky_hi) stage_lab(ky + 2, (i + 2) % 3);
+            const int lnext = (i + 1) % 3;
+            const float *Cs = asm_ + b * CS, *wRs = wR0 + b * e * kAwTX, *wTs = wT0 + b * e * NTP;
+            float *wRn = wR0 + (b ^ 1) * e * kAwTX, *wTn = wT0 + (b ^ 1) * e * NTP;
+
+            const int ubase = px0 - 4 * td + kAwDC - 4;
+            const float *cp = Cs + px0 * kAwCPitch + 4 * td;
+            const float *wrp = wRs + px0;
+            const float *wtp = wTs + ubase;
+            auto tap = [&](const float (*cw)[4], int cofs, const float *wr4, const float *wt7) {
+                float wr[4], wt[7];
+                const float4 a0 = *reinterpret_cast<const float4 *>(wr4);
+                wr[0] = a0.x; wr[1] = a0.y; wr[2] = a0.z; wr[3] = a0.w;
+                const float4 b0 = *reinterpret_cast<const float4 *>(wt7);
+                const float4 b1 = *reinterpret_cast<const float4 *>(wt7 + 4);
+                wt[0] = b0.x; wt[1] = b0.y; wt[2] = b0.z; wt[3] = b0.w;
+                wt[4] = b1.x; wt[5] = b1.y; wt[6] = b1.z;
+#pragma unroll
+                for (int j = 0; j < 4; j++)
+#pragma unroll
+                    for (int h = 0; h < 2; h++) {
+                        const unsigned long long w = pack2(__fmul_rn(wr[j], wt[j - 2 * h + 3]),
+                                                           __fmul_rn(wr[j], wt[j - 2 * h + 2]));
+                        const unsigned long long c = pack2(cw[j + cofs][2 * h], cw[j + cofs][2 * h + 1]);
+                        sw[j][h] = add2(sw[j][h], w);
+                        sc[j][h] = add2(sc[j][h], mul2(c, w));
+                    }
+            };
+            int kx = 0, sj = 0;
+#pragma unroll 1
+            for (; kx + 4 <= e; kx += 4, cp += 4 * kAwCPitch, wrp += 4 * kAwTX, wtp += 4 * NTP, sj++) {
+                // a slice of the next tap row's weights around this group of taps
+                const int ks = warp + NW * sj;
+                const bool dos = next && ks < e;
+                Slice sl;
+                if (dos) slice_issue(sl, ky + 1, ks, lnext);
+                float cw[7][4];
+#pragma unroll
+                for (int q = 0; q < 7; q++) {
+                    const float4 v = *reinterpret_cast<const float4 *>(cp + q * kAwCPitch);
+                    cw[q][0] = v.x; cw[q][1] = v.y; cw[q][2] = v.z; cw[q][3] = v.w;
+                }
+#pragma unroll
+                for (int u = 0; u < 4; u++) tap(cw, u, wrp + u * kAwTX, wtp + u * NTP);
+                if (dos) slice_finish(sl, ky + 1, ks, wRn, wTn);
+            }
+#pragma unroll 1
+            for (; kx < e; kx++, cp += kAwCPitch, wrp += kAwTX, wtp += NTP) {
+                float cw[4][4];
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    const float4 v = *reinterpret_cast<const float4 *>(cp + q * kAwCPitch);
+                    cw[q][0] = v.x; cw[q][1] = v.y; cw[q][2] = v.z; cw[q][3] = v.w;
+                }
+                tap(cw, 0, wrp, wtp);
+            }
+            // slices the groups did not reach (short windows)
+            if (next)
+                for (int ks = warp + NW * sj; ks < e; ks += NW) {
+                    Slice sl;
+                    slice_issue(sl, ky + 1, ks, lnext);
+                    slice_finish(sl, ky + 1, ks, wRn, wTn);
+                }
+            asm volatile("cp.async.wait_all;\n" ::: "memory");
+            __syncthreads();
+        }
+        // score / sum of weights (seq/AdaptiveWeightAggregation.cpp:108), staged for the arg-min
+        float *outs = asm_;  // [64][kAwDC + 1]
+#pragma unroll
+        for (int j = 0; j < 4; j++)
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                const float v = __fdiv_rn(half2_of(sc[j][i >> 1], i & 1), half2_of(sw[j][i >> 1], i & 1));
+                outs[(px0 + j) * (kAwDC + 1) + 4 * td + i] = v;
+                const int x = x0 + px0 + j, dg = dc0 + 4 * td + i;
+                if (cost_out && x < W && dg < D) cost_out[((size_t)y * W + x) * D + dg] = v;
+            }
+        __syncthreads();
+        if (tid < kAwTX) {
+            float bv = best_v[tid];
+            int bx = best_i[tid];
+            const int nd = imin(kAwDC, D - dc0);
+            for (int dd = 0; dd < nd; dd++) {
+                const float v = outs[tid * (kAwDC + 1) + dd];
+                if (v < bv) {  // first strict minimum in increasing d
+                    bv = v;
+                    bx = dc0 + dd;
+                }
+            }
+            best_v[tid] = bv;
+            best_i[tid] = bx;
+        }
+    }
+    if (tid < kAwTX && x0 + tid < W) {
+        const int x = x0 + tid;
+        const bool found = best_i[tid] != 0;
+        raw[(size_t)y * W + x] = found ? (uint16_t)(0x100 | best_i[tid]) : (uint16_t)0;
+        if (found) atomicMax(row_last + y, x);
+    }
+}
+
+// ---------------------------------------------------------------------------
 // host orchestration
 
 static bool fast_kind(int k) { return k == RTS_COST_AD || k == RTS_COST_CENSUS; }
@@ -458,9 +724,18 @@ rts_status aw_fused(rts_ctx *c, const rts_params &p, int H, int W, const void *v
         cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         kern<<<grid, kAwThreads, smem, c->stream>>>(v, plr, plt, pw, g, raw, rl, cost_out, H, W, p.disp_range, e);
     };
-    // plain form: bit-exact float volume; FP16 form: __half volume and fused multiply-add
-    if (half) go(k_aw_wta<__half, false>, (const __half *)vol);
-    else go(k_aw_wta<float, true>, (const float *)vol);
+    // plain form: bit-exact float volume, the pipelined kernel; FP16 form: __half
+    // volume and fused multiply-add
+    if (half) {
+        go(k_aw_wta<__half, false>, (const __half *)vol);
+    } else {
+        const size_t psmem = sizeof(float) * (2 * (size_t)(kAwTX + 2 * r + 4) * kAwCPitch + 2 * (size_t)e * kAwTX +
+                                              2 * (size_t)e * (kAwTX + kAwDC)) +
+                             sizeof(uint32_t) * 3 * ((size_t)(kAwTX + 2 * r) + (size_t)(kAwTX + kAwDC - 1 + 2 * r));
+        cudaFuncSetAttribute(k_aw_wta_pipe<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)psmem);
+        k_aw_wta_pipe<0><<<grid, kAwThreads, psmem, c->stream>>>((const float *)vol, plr, plt, pw, g, raw, rl, cost_out,
+                                                                 H, W, p.disp_range, e);
+    }
     count_launch(c);
     return check_launch(c, "aw_wta");
 }
