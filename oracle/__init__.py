@@ -60,6 +60,7 @@ _ORACLE_SIGS = {
     "orc_disp_refinement_oop": [_p, _p, _p, _p, _i, _i, _i],
     "orc64_combine": [_p, _p, _d, _d, _l, _p],
     "orc64_aw_l2r": [_p, _p, _p, _p, _i, _i, _i, _i, _d, _d],
+    "orc64_aw_l2r_pre": [_p, _p, _p, _p, _i, _i, _i, _i, _d, _d],
     "orc64_ncc": [_p, _p, _p, _i, _i, _i, _i, _i],
     "orc64_convolve": [_p, _p, _p, _i, _i, _i, _i],
     "orc_pipeline": [_p, _i, _i, _p, _p, _p, _p, _p, _p, _p, _p, _p, _p],
@@ -102,7 +103,7 @@ def _bind(lib, sigs):
     for name, args in sigs.items():
         fn = getattr(lib, name)
         fn.argtypes = args
-        fn.restype = _i if name == "orc_pipeline" else None
+        fn.restype = _i if name in ("orc_pipeline", "orc64_aw_l2r_pre") else None
     return lib
 
 
@@ -327,6 +328,16 @@ def f64_aw_l2r(labr, labt, cost, rad, gamma_s, gamma_p):
     H, W, D = cost.shape
     out = np.empty(cost.shape, np.float64)
     lib().orc64_aw_l2r(ptr(labr), ptr(labt), ptr(cost), ptr(out), H, W, D, rad, gamma_s, gamma_p)
+    return out
+
+
+def f64_aw_l2r_pre(labr, labt, cost64, rad, gamma_s, gamma_p):
+    """FP64 adaptive-weight aggregation of an FP64 volume (weights made once per pixel)."""
+    cost64 = np.ascontiguousarray(cost64, np.float64)
+    H, W, D = cost64.shape
+    out = np.empty_like(cost64)
+    if lib().orc64_aw_l2r_pre(ptr(labr), ptr(labt), ptr(cost64), ptr(out), H, W, D, rad, gamma_s, gamma_p) != 0:
+        raise MemoryError("orc64_aw_l2r_pre")
     return out
 
 

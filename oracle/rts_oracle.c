@@ -587,6 +587,55 @@ void orc64_aw_l2r(const uint8_t *labr, const uint8_t *labt, const float *cost, d
         }
 }
 
+/* The same FP64 aggregation as orc64_aw_l2r over an FP64 cost volume, with
+ * every pixel's weights computed once (the sums in the same tap order). */
+int orc64_aw_l2r_pre(const uint8_t *labr, const uint8_t *labt, const double *cost, double *out,
+                     int H, int W, int D, int rad, double gamma_s, double gamma_p) {
+    int edge = 2 * rad + 1;
+    long E = (long)edge * edge, np = (long)H * W;
+    double *wr = (double *)malloc(sizeof(double) * np * E), *wt = (double *)malloc(sizeof(double) * np * E);
+    if (!wr || !wt) { free(wr); free(wt); return -1; }
+    for (int pass = 0; pass < 2; pass++) {
+        const uint8_t *lab = pass ? labt : labr;
+        double *w = pass ? wt : wr;
+        for (int y = 0; y < H; y++)
+            for (int x = 0; x < W; x++) {
+                long p = (long)y * W + x, k = 0;
+                for (int dy = -rad; dy <= rad; dy++)
+                    for (int dx = -rad; dx <= rad; dx++, k++) {
+                        int yy = y + dy, xx = x + dx;
+                        double v = 0;
+                        if (yy >= 0 && yy < H && xx >= 0 && xx < W) {
+                            const uint8_t *a = lab + 3 * p, *b = lab + 3 * ((long)yy * W + xx);
+                            double e = sqrt((double)(a[0] - b[0]) * (a[0] - b[0]) + (double)(a[1] - b[1]) * (a[1] - b[1]) +
+                                            (double)(a[2] - b[2]) * (a[2] - b[2]));
+                            v = exp(-sqrt((double)(dy * dy + dx * dx)) / gamma_p) * exp(-e / gamma_s);
+                        }
+                        w[p * E + k] = v;
+                    }
+            }
+    }
+    for (int y = 0; y < H; y++)
+        for (int x = 0; x < W; x++) {
+            long p = (long)y * W + x;
+            for (int d = 0; d < D; d++) {
+                long t = (long)y * W + tar_col(x, d, W, ORC_L2R);
+                double sw = 0, sc = 0;
+                long k = 0;
+                for (int dy = -rad; dy <= rad; dy++)
+                    for (int dx = -rad; dx <= rad; dx++, k++) {
+                        double wgt = wr[p * E + k] * wt[t * E + k];
+                        sw += wgt;
+                        sc += wgt * cost[d + (long)D * ((long)wrap1(y + dy, H) * W + wrap1(x + dx, W))];
+                    }
+                out[d + (long)D * p] = sc / sw;
+            }
+        }
+    free(wr);
+    free(wt);
+    return 0;
+}
+
 void orc64_ncc(const uint8_t *ref, const uint8_t *tar, double *cost, int D, int H, int W, int hrad, int wrad) {
     int area = (2 * hrad + 1) * (2 * wrad + 1);
     for (int y = 0; y < H; y++)

@@ -59,6 +59,8 @@ void orc_disp_refinement_oop(const uint8_t *disp, uint8_t *out, const int *horz,
 void orc64_combine(const float *c1, const float *c2, double lambda1, double lambda2, long n, double *out);
 void orc64_aw_l2r(const uint8_t *labr, const uint8_t *labt, const float *cost, double *out,
                   int H, int W, int D, int rad, double gamma_s, double gamma_p);
+int orc64_aw_l2r_pre(const uint8_t *labr, const uint8_t *labt, const double *cost, double *out,
+                     int H, int W, int D, int rad, double gamma_s, double gamma_p);
 void orc64_ncc(const uint8_t *ref, const uint8_t *tar, double *cost, int D, int H, int W, int hrad, int wrad);
 void orc64_convolve(const uint8_t *img, double *out, const float *mask, int H, int W, int hrad, int wrad);
 

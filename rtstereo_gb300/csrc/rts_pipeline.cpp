@@ -258,7 +258,7 @@ static rts_status view_composed(rts_ctx *c, const rts_params &p, int H, int W, c
 
 // Fused path for one view (cross-based or adaptive-weight aggregation).
 static rts_status view_fused(rts_ctx *c, const rts_params &p, int H, int W, const ViewIn &v, uint8_t *disp,
-                             int mirror) {
+                             int mirror, float *cost_out) {
     const int D = p.disp_range;
     const size_t np = (size_t)H * W, ne = np * D;
     cudaStream_t s = c->stream;
@@ -290,7 +290,7 @@ static rts_status view_fused(rts_ctx *c, const rts_params &p, int H, int W, cons
         }
         vol = c1v;
     }
-    RTS_TRY(aw_fused(c, p, H, W, vol, vol_half, v.lref, v.ltar, (uint16_t *)raw, (int *)rl, nullptr));
+    RTS_TRY(aw_fused(c, p, H, W, vol, vol_half, v.lref, v.ltar, (uint16_t *)raw, (int *)rl, cost_out));
     {
         StageScope sc(c, "wta_fill");
         launch_wta_fill(s, (const uint16_t *)raw, (const int *)rl, disp, H, W, mirror);
@@ -301,7 +301,9 @@ static rts_status view_fused(rts_ctx *c, const rts_params &p, int H, int W, cons
 
 rts_status run_view(rts_ctx *c, const rts_params &p, int H, int W, const ViewIn &v, uint8_t *disp, int mirror,
                     float *cost_out) {
-    if (!cost_out && p.aggr == RTS_AGGR_AW && fused_supported(p, H, W)) return view_fused(c, p, H, W, v, disp, mirror);
+    // the FP16 form's final volume comes from its own (fused) kernel
+    if (p.aggr == RTS_AGGR_AW && fused_supported(p, H, W) && (!cost_out || p.precision == RTS_PREC_F16))
+        return view_fused(c, p, H, W, v, disp, mirror, cost_out);
     return view_composed(c, p, H, W, v, disp, mirror, cost_out);
 }
 
@@ -491,7 +493,8 @@ rts_status rts_pipeline_run(rts_ctx *ctx, rts_mem m, const rts_pair *pair, const
     if (!pair->left_gray || !pair->right_gray || !out->disp_left) return set_error(c, RTS_ERR_INVALID_ARG, "null image or output");
     if (p.right_view && (!out->disp_right || !out->mask)) return set_error(c, RTS_ERR_INVALID_ARG, "right view needs disp_right and mask");
     if (p.aggr == RTS_AGGR_AW && (!pair->left_lab || !pair->right_lab)) return set_error(c, RTS_ERR_INVALID_ARG, "adaptive weights need Lab images");
-    if (out->cost_left && p.precision != RTS_PREC_F32) return set_error(c, RTS_ERR_INVALID_ARG, "cost_left is available in the plain form only");
+    if (out->cost_left && p.precision != RTS_PREC_F32 && !(p.aggr == RTS_AGGR_AW && fused_supported(p, H, W)))
+        return set_error(c, RTS_ERR_INVALID_ARG, "cost_left: the plain form, or the FP16 form of adaptive weights");
     const size_t np = (size_t)H * W, ne = np * p.disp_range;
     const uint8_t *lg, *rg, *lc = nullptr, *rc = nullptr, *ll = nullptr, *rl = nullptr;
     const void *t;
