@@ -14,6 +14,12 @@
 // budget) are free; admitted requests are launched as batches on a ring of
 // streams, so a batch formed from requests that arrived while others were
 // running overlaps with them on the device.  Completion is polled with events.
+// With priority_pixels, requests of at least that many pixels form a second
+// class: each runs alone on a stream of the greatest priority, while the other
+// class's batches run one block per work item, so the large request's blocks
+// are dispatched as soon as the small ones' retire.  Pinned host staging is
+// kept in a cache across requests (pinning pages is slow, and freeing them
+// waits for the device).
 #include <string.h>
 
 #include <chrono>

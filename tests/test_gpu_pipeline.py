@@ -125,6 +125,26 @@ def test_fused_paths_match_oracle(ctx, oracle_mod):
         assert_same(g, o)
 
 
+@pytest.mark.parametrize("W,H,D,rad", [(70, 9, 30, 5), (40, 20, 13, 16), (130, 7, 64, 1), (200, 12, 128, 3),
+                                       (72, 40, 66, 16)])
+def test_fused_adaptive_weight_shapes(ctx, oracle_mod, W, H, D, rad):
+    """The fused adaptive-weight kernels (plain and pipelined tap rows) on colour
+    inputs: disparity ranges that are not multiples of 4 (word-wise cost copies)
+    or span two 64-disparity chunks, windows taller than the image, one-row
+    windows, widths that are not multiples of the 64-pixel tile."""
+    import rtstereo_gb300 as R
+    O = oracle_mod
+    L, Rr = synth(W * 7 + D, W, H, D, 3)
+    rng = np.random.default_rng(W + H)
+    Lc = np.ascontiguousarray(np.stack([L, rng.integers(0, 256, (H, W), dtype=np.uint8), 255 - L], -1))
+    Rc = np.ascontiguousarray(np.stack([Rr, rng.integers(0, 256, (H, W), dtype=np.uint8), 255 - Rr], -1))
+    lab = (R.rgb_to_lab(Lc), R.rgb_to_lab(Rc))
+    p = R.params(disp_range=D, aggr=2, aw_rad=rad)
+    g = ctx.pipeline(p, L, Rr, Lc, Rc, *lab)
+    o = O.pipeline(O.params(D=D, aggr=2, aw_rad=rad), L, Rr, Lc, Rc, *lab)
+    assert bits_equal(g[0], o[0]) and bits_equal(g[1], o[1]) and bits_equal(g[2], o[2])
+
+
 @pytest.mark.parametrize("name,c1,c2,ag,D", [("pipe_ad_census_cross", 1, 3, 3, 16),
                                               ("pipe_rank_census_aw", 2, 3, 2, 6)])
 def test_golden_pipelines(ctx, golden, name, c1, c2, ag, D):
