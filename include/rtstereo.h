@@ -251,7 +251,10 @@ typedef struct rts_request_stats {
 
 rts_status rts_server_create(rts_server **out, rts_ctx *ctx, const rts_server_config *cfg);
 void rts_server_destroy(rts_server *s);
-/* Copies the HOST inputs (pair) on submit; outputs land in HOST out buffers. */
+/* Copies the HOST inputs (pair) on submit; outputs land in HOST out buffers
+ * (pinned ones are written by the device directly, pageable ones through the
+ * server's pinned staging; a cancelled request that is already running may
+ * still write pinned outputs). */
 rts_status rts_server_submit(rts_server *s, const rts_pair *pair, const rts_params *params, rts_out *out,
                              uint64_t *ticket);
 /* 1 done, 0 pending, <0 an error status (negated) */

@@ -358,11 +358,14 @@ class Server:
         except Exception:
             pass
 
-    def submit(self, p: Params, lgray, rgray, lrgb=None, rrgb=None):
-        """Queues a pair (HOST arrays, copied now); returns (ticket, (disp_l, disp_r, mask))."""
+    def submit(self, p: Params, lgray, rgray, lrgb=None, rrgb=None, outs=None):
+        """Queues a pair (HOST arrays, copied now); returns (ticket, (disp_l, disp_r, mask)).
+        outs: optional three [H][W] u8 arrays to receive the results (pinned ones are
+        written by the device directly)."""
         H, W = lgray.shape
         pair = Pair(W, H, _ptr(lgray), _ptr(rgray), _ptr(lrgb), _ptr(rrgb), None, None)
-        outs = tuple(np.zeros((H, W), np.uint8) for _ in range(3))
+        if outs is None:
+            outs = tuple(np.zeros((H, W), np.uint8) for _ in range(3))
         out = Out(_ptr(outs[0]), _ptr(outs[1]), _ptr(outs[2]), None)
         t = C.c_uint64()
         st = self._lib.rts_server_submit(self.h, C.byref(pair), C.byref(p), C.byref(out), C.byref(t))

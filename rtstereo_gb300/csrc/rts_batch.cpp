@@ -407,6 +407,7 @@ struct Request {
                                     // then, in the same staging block, h_out
     unsigned char *h_out = nullptr; // pinned outputs: disp L, disp R, mask
     size_t in_bytes = 0, out_bytes = 0;
+    bool direct_out = false;   // the caller's output buffers are pinned: the device writes them directly
     void *d_mem = nullptr;     // device: inputs + outputs
     size_t d_bytes = 0;
     int state = RQ_PENDING;
@@ -461,10 +462,12 @@ void finish_batch(rts_server *s, Batch &bt) {
         Request &r = *it->second;
         const size_t np = (size_t)r.pair.width * r.pair.height;
         if (r.state == RQ_RUNNING) {
-            memcpy(r.out.disp_left, r.h_out, np);
-            if (r.params.right_view) {
-                memcpy(r.out.disp_right, r.h_out + np, np);
-                memcpy(r.out.mask, r.h_out + 2 * np, np);
+            if (!r.direct_out) {
+                memcpy(r.out.disp_left, r.h_out, np);
+                if (r.params.right_view) {
+                    memcpy(r.out.disp_right, r.h_out + np, np);
+                    memcpy(r.out.mask, r.h_out + 2 * np, np);
+                }
             }
             r.state = RQ_DONE;
         }
@@ -564,8 +567,20 @@ rts_status launch_batch(rts_server *s, std::vector<Request *> &ids) {
     }
     for (int i = 0; i < n && st == RTS_OK; i++) {
         Request &r = *ids[i];
-        if (cudaMemcpyAsync(r.h_out, outs[i].disp_left, r.out_bytes, cudaMemcpyDeviceToHost, c->stream) != cudaSuccess)
-            st = set_error(c, RTS_ERR_CUDA, "server D2H copy failed");
+        const size_t np = (size_t)r.pair.width * r.pair.height;
+        bool ok;
+        if (r.direct_out) {
+            ok = cudaMemcpyAsync(r.out.disp_left, outs[i].disp_left, np, cudaMemcpyDeviceToHost, c->stream) ==
+                     cudaSuccess &&
+                 (!r.params.right_view ||
+                  (cudaMemcpyAsync(r.out.disp_right, outs[i].disp_right, np, cudaMemcpyDeviceToHost, c->stream) ==
+                       cudaSuccess &&
+                   cudaMemcpyAsync(r.out.mask, outs[i].mask, np, cudaMemcpyDeviceToHost, c->stream) == cudaSuccess));
+        } else {
+            ok = cudaMemcpyAsync(r.h_out, outs[i].disp_left, r.out_bytes, cudaMemcpyDeviceToHost, c->stream) ==
+                 cudaSuccess;
+        }
+        if (!ok) st = set_error(c, RTS_ERR_CUDA, "server D2H copy failed");
     }
     if (st == RTS_OK && cudaEventRecord(bt.done, c->stream) != cudaSuccess) st = RTS_ERR_CUDA;
     c->stream = saved;
@@ -721,6 +736,16 @@ rts_status rts_server_submit(rts_server *s, const rts_pair *pair, const rts_para
     r->pair.right_rgb = rgb ? pair->right_rgb : nullptr;
     r->in_bytes = np * (rgb ? 8 : 2);
     r->out_bytes = np * 3;
+    // pinned (page-locked) output buffers are written by the device directly
+    auto pinned = [](const void *q) {
+        cudaPointerAttributes a;
+        if (cudaPointerGetAttributes(&a, q) != cudaSuccess) {
+            cudaGetLastError();
+            return false;
+        }
+        return a.type == cudaMemoryTypeHost;
+    };
+    r->direct_out = pinned(out->disp_left) && (!params->right_view || (pinned(out->disp_right) && pinned(out->mask)));
     // admission control also covers requests that could never fit
     int Wv[2] = {pair->width, pair->width}, Hv[2] = {pair->height, pair->height},
         Dv[2] = {params->disp_range, params->disp_range};

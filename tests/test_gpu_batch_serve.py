@@ -64,18 +64,23 @@ def test_batch_matches_single_runs(ctx, oracle_mod, prec):
         assert all(bits_equal(a, b) for a, b in zip(g, o[:3]))
 
 
-@pytest.mark.parametrize("priority_pixels", [0, 128 * 128])
-def test_server_same_alone_and_in_the_mix(ctx, priority_pixels):
+@pytest.mark.parametrize("priority_pixels,pinned", [(0, False), (128 * 128, False), (128 * 128, True)])
+def test_server_same_alone_and_in_the_mix(ctx, priority_pixels, pinned):
     """With priority_pixels the larger pairs of the mix run alone on high-priority
-    streams while the smaller ones are batched; results do not change."""
+    streams while the smaller ones are batched; with pinned result buffers the
+    device writes them directly; results do not change."""
     import rtstereo_gb300 as R
+    torch = pytest.importorskip("torch") if pinned else None
     srv = R.Server(ctx, hbm_budget=1 << 30, max_inflight=8, max_batch=3, precision=R.PREC_F16,
                    priority_pixels=priority_pixels)
     try:
         data = make_pairs(55) * 3
         tickets = []
         for L, Rr, D in data:
-            tickets.append(srv.submit(R.params(disp_range=D, precision=R.PREC_F16), L, Rr))
+            outs = None
+            if pinned:
+                outs = tuple(torch.full(L.shape, 77, dtype=torch.uint8).pin_memory().numpy() for _ in range(3))
+            tickets.append(srv.submit(R.params(disp_range=D, precision=R.PREC_F16), L, Rr, outs=outs))
             srv.progress()
         stats = [srv.wait(t) for t, _ in tickets]
         for (L, Rr, D), (t, outs) in zip(data, tickets):
