@@ -83,3 +83,36 @@ def test_driver_matches_oracle_left_view(tmp_path, oracle_mod, args):
     O = oracle_mod
     dl, _, _, _ = O.pipeline(O.params(cost1=c1, cost2=c2, aggr=ag, D=D), L, Rr, Lc, Rc)
     assert np.array_equal(got, _scale_like_driver(dl, D, auto))
+
+
+def _write_ppm(path, rgb):
+    with open(path, "wb") as f:
+        f.write(b"P6\n%d %d\n255\n" % (rgb.shape[1], rgb.shape[0]))
+        f.write(np.ascontiguousarray(rgb, np.uint8).tobytes())
+
+
+@pytest.mark.gpu
+def test_driver_colour_inputs(tmp_path, oracle_mod):
+    """PPM inputs: the colour image feeds AD and the cross arms, its BT.601 luma
+    (14-bit fixed point, as the driver converts) the gray costs."""
+    import rtstereo_gb300 as R
+    D, W, H = 16, 80, 40
+    L, Rr, _ = R.synth_pair(0xC7, W, H, D, 4, 0, 2.0, 4)
+    rng = np.random.default_rng(7)
+    mk = lambda g: np.ascontiguousarray(np.stack([g, (g.astype(np.int32) * 3 // 4).astype(np.uint8),
+                                                  np.clip(g.astype(np.int32) + rng.integers(-20, 21, g.shape), 0,
+                                                          255).astype(np.uint8)], -1))
+    Lc, Rc = mk(L), mk(Rr)
+    _write_ppm(tmp_path / "l.ppm", Lc)
+    _write_ppm(tmp_path / "r.ppm", Rc)
+    name = str(tmp_path / "c")
+    r = subprocess.run([_driver(), str(tmp_path / "l.ppm"), str(tmp_path / "r.ppm"), str(D), "1", "3", "3", "0",
+                        "10", "10", name], capture_output=True, text=True)
+    assert r.returncode == 1, r.stdout
+    got = _read_png_gray(f"{name}_1_3_3_0_10_10.png")
+    def luma(c):
+        c = c.astype(np.uint32)
+        return ((4899 * c[..., 0] + 9617 * c[..., 1] + 1868 * c[..., 2] + 8192) >> 14).astype(np.uint8)
+    O = oracle_mod
+    dl, _, _, _ = O.pipeline(O.params(D=D, right_view=0), luma(Lc), luma(Rc), Lc, Rc)
+    assert np.array_equal(got, _scale_like_driver(dl, D, 0))
