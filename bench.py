@@ -576,8 +576,9 @@ def run_ours(args, rank, world):
 # of each at 1280x720, D=128 (both views; profiles/cross_views_*.md); a launch at
 # another size moves these per entry
 NCU_BYTES_PER_ENTRY = {("cross_vert_wta", 0): 4.16, ("cross_hseg", 0): 4.00}
-# ncu DRAM bytes of one k_aw_wta launch (one view) at 640x480, D=64 (profiles/k_aw_wta_*.md)
-NCU_AW_BYTES = {(640, 480, 64): 85.57e6}
+# ncu DRAM bytes of one plain-form adaptive-weight launch (k_aw_wta_pipe, one view)
+# at 640x480, D=64 (profiles/k_aw_wta_pipe_*.md)
+NCU_AW_BYTES = {(640, 480, 64): 85.52e6}
 
 
 def roofline(stages, name, W, H, D, ag, peaks, src, p, ms_pair=None):
@@ -597,8 +598,8 @@ def roofline(stages, name, W, H, D, ag, peaks, src, p, ms_pair=None):
         achieved = flops / (per_launch_ms / 1e3) / 1e12
         mhz = peaks.get("sm_max_mhz", 2070.0)
         peak = 152 * 128 * mhz * 1e6 / 1e12  # one FP32 op per lane per clock (unfused ops)
-        traffic = NCU_AW_BYTES.get((W, H, D))
-        return {"bound": "fp32", "kernel": "k_aw_wta", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+        traffic = NCU_AW_BYTES.get((W, H, D)) if not p.precision else None
+        return {"bound": "fp32", "kernel": "k_aw_wta" if p.precision else "k_aw_wta_pipe", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                 "frac": achieved / peak, "traffic": traffic, "launches": launches, "ms_per_launch": per_launch_ms,
                 "flop_per_launch": flops,
                 "peak_source": f"FP32 pipe, unfused operations: 152 SMs x 128 lanes x {mhz:.0f} MHz "
