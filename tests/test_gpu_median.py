@@ -117,3 +117,27 @@ def test_median_option_validated(ctx):
             ctx.pipeline(R.params(disp_range=8, **kw), L, L)
     with pytest.raises(R.RtsError):
         ctx.medianFilt(np.zeros((4, 4), np.uint8), 2)
+
+
+def test_fp16_server_with_median_and_priority(ctx):
+    """FP16 form, median-filtered arms, the priority class and pinned results in
+    the serving loop: every result equals the single-pair run of the same form."""
+    torch = pytest.importorskip("torch")
+    import rtstereo_gb300 as R
+    shapes = [(160, 120, 32), (96, 64, 64), (200, 90, 16), (128, 100, 48)]
+    data = [colour_pair(0x6E0 + i, W, H, D) + (D,) for i, (W, H, D) in enumerate(shapes)]
+    mk = lambda D: R.params(disp_range=D, median_ksize=3, precision=R.PREC_F16)
+    want = [ctx.pipeline(mk(D), L, Rr, Lc, Rc)[:3] for L, Rr, Lc, Rc, D in data]
+    srv = R.Server(ctx, hbm_budget=1 << 30, max_inflight=4, max_batch=2, precision=R.PREC_F16,
+                   priority_pixels=150 * 100)
+    try:
+        tickets = []
+        for L, Rr, Lc, Rc, D in data * 2:
+            outs = tuple(torch.zeros(L.shape, dtype=torch.uint8).pin_memory().numpy() for _ in range(3))
+            tickets.append(srv.submit(mk(D), L, Rr, Lc, Rc, outs=outs))
+        for t, _ in tickets:
+            srv.wait(t)
+        for (t, outs), w in zip(tickets, want * 2):
+            assert all(bits_equal(a, b) for a, b in zip(outs, w))
+    finally:
+        srv.close()
