@@ -59,6 +59,75 @@ def make_inputs(name):
     return (W, H, D, c1, c2, ag, extra), (L, Rr, Lc, Rc, Ll, Rl)
 
 
+def f64_aw_rows(L, Rr, Lc, Rc, Ll, Rl, D, rad, gamma_s, gamma_p, lam1, lam2, rows, hr, wr):
+    """FP64 adaptive-weight costs of the left view on a few rows, in numpy: the
+    same terms as the pipeline (colour SAD and census 9x7 Hamming distance, both
+    exact integers, combined as (1 - exp(-a/l1)) + (1 - exp(-h/l2)), then the
+    weighted average over the (2 rad + 1)^2 window), every operation in double."""
+    H, W = L.shape
+    ys, xs = np.arange(H), np.arange(W)
+
+    def census(img):
+        # the census code of every pixel packed into a u64 (strict centre > neighbour)
+        g = img.astype(np.int16)
+        code = np.zeros((H, W), np.uint64)
+        k = 0
+        for dy in range(-hr, hr + 1):
+            for dx in range(-wr, wr + 1):
+                code |= (g > g[(ys + dy) % H][:, (xs + dx) % W]).astype(np.uint64) << np.uint64(k)
+                k += 1
+        return code
+
+    pop8 = np.array([bin(i).count("1") for i in range(256)], np.int32)
+    cl, cr = census(L), census(Rr)
+    dys, dxs = np.meshgrid(np.arange(-rad, rad + 1), np.arange(-rad, rad + 1), indexing="ij")
+    dys, dxs = dys.ravel(), dxs.ravel()
+    prox = np.exp(-np.sqrt((dys * dys + dxs * dxs).astype(np.float64)) / gamma_p)
+    out = np.empty((len(rows), W, D))
+    for i, y in enumerate(rows):
+        band = (y + np.arange(-rad, rad + 1)) % H
+        # combined costs of the band's rows: [row][x][d]
+        xt = (xs[:, None] - np.arange(D)[None, :]) % W
+        sad = np.abs(Lc[band][:, :, None, :].astype(np.int32) - Rc[band][:, xt, :].astype(np.int32)).sum(-1)
+        ham = pop8[(cl[band][:, :, None] ^ cr[band][:, xt]).view(np.uint8)].reshape(len(band), W, D, 8).sum(-1)
+        cost = (1.0 - np.exp(-sad / lam1)) + (1.0 - np.exp(-ham / lam2))
+
+        def weights(lab):
+            yy, xx = y + dys[None, :], xs[:, None] + dxs[None, :]
+            ok = (yy >= 0) & (yy < H) & (xx >= 0) & (xx < W)
+            q = lab[np.clip(yy, 0, H - 1), np.clip(xx, 0, W - 1)].astype(np.float64)
+            e = np.sqrt(((q - lab[y][:, None, :].astype(np.float64)) ** 2).sum(-1))
+            return np.where(ok, prox[None, :] * np.exp(-e / gamma_s), 0.0)
+
+        wr_, wt_ = weights(Ll), weights(Rl)
+        rpos = dys + rad
+        cols = (xs[:, None] + dxs[None, :]) % W
+        for d in range(D):
+            w = wr_ * wt_[(xs - d) % W]
+            c = cost[rpos[None, :], cols, d]
+            out[i, :, d] = (w * c).sum(1) / w.sum(1)
+    return out
+
+
+def aw_cost_error_vs_f64(ctx, R, p16, p32, L, Rr, Lc, Rc, Ll, Rl):
+    """Max error of the FP16 form's (and the plain form's) final left cost volume
+    against FP64, relative to the largest FP64 cost, on four sampled rows."""
+    H, W = L.shape
+    D = p16.disp_range
+    rows = [H // 8, 3 * H // 8, 5 * H // 8, 7 * H // 8]
+    got = {}
+    for k, p in (("f16", p16), ("f32", p32)):
+        pr = R.params(**{f: getattr(p, f) for f, _ in R.Params._fields_})
+        pr.right_view = 0
+        got[k] = ctx.pipeline(pr, L, Rr, Lc, Rc, Ll, Rl, want_cost=True)[3][rows]
+    ref = f64_aw_rows(L, Rr, Lc, Rc, Ll, Rl, D, p16.aw_rad, p16.aw_gamma_s, p16.aw_gamma_p, p16.lambda1, p16.lambda2,
+                      rows, p16.census_hrad, p16.census_wrad)
+    scale = float(np.abs(ref).max())
+    return {"rows": rows, "f16_max_abs": float(np.abs(got["f16"] - ref).max()),
+            "f16_max_rel": float(np.abs(got["f16"] - ref).max() / scale),
+            "f32_max_rel": float(np.abs(got["f32"] - ref).max() / scale)}
+
+
 def measured_peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -540,6 +609,8 @@ def run_ours(args, rank, world):
         f16_agree = {"disp_left": float((ref[0].numpy() == ho[0].numpy()).mean()),
                      "disp_right": float((ref[1].numpy() == ho[1].numpy()).mean()),
                      "mask": float((ref[2].numpy() == ho[2].numpy()).mean())}
+        if ag == 2 and rank == 0:
+            f16_agree["cost_error_vs_f64"] = aw_cost_error_vs_f64(ctx, R, p, p32, L, Rr, Lc, Rc, Ll, Rl)
 
     if rank != 0:
         ranks_done(world)
