@@ -44,6 +44,7 @@ WORKLOADS = {
     "rank_census_cross_1920x1080_d128": (1920, 1080, 128, 2, 3, 3, 24, 2, 3.0, 0xC2, {"rank_rad": 3}),
     "box_1920x1080_d128": (1920, 1080, 128, 1, 3, 1, 24, 2, 3.0, 0xC2, {"box_rad": 4}),
     "log_census_cross_1920x1080_d128": (1920, 1080, 128, 4, 3, 3, 24, 2, 3.0, 0xC2, {}),
+    "census_cross_1920x1080_d128": (1920, 1080, 128, 3, 0, 3, 24, 2, 3.0, 0xC2, {}),
     "ncc_box_1920x1080_d128": (1920, 1080, 128, 5, 0, 1, 24, 2, 3.0, 0xC2, {"box_rad": 4, "ncc_hrad": 3,
                                                                             "ncc_wrad": 3}),
 }
@@ -679,7 +680,9 @@ def roofline(stages, name, W, H, D, ag, peaks, src, p, ms_pair=None):
     # times per view at S bytes an entry; the row-segment kernel owns the first two
     # crossings (written by matching and combining, read by aggregation), the
     # vertical kernel the last two (written by aggregation, read by WTA)
-    S = 2 if p.precision else 4
+    # integer costs (census or truncated AD alone) keep u16 segments in both forms
+    int_costs = p.cost2 == 0 and (p.cost1 == 3 or (p.cost1 == 1 and float(p.ad_trunc).is_integer()))
+    S = 2 if (p.precision or int_costs) else 4
     views = 2
     byts = views * 2 * S * E
     achieved = byts / (per_launch_ms / 1e3) / 1e9

@@ -192,7 +192,8 @@ constexpr int kHLag = 24;   // columns between a column's prefix and its segment
 constexpr int kHSub = 8;    // columns per group
 
 // MODE: 0 precomputed volume, 1 truncated AD + census through the combined host
-// table (the configuration of the cross-based pipeline), 2 any AD/census pair
+// table (the configuration of the cross-based pipeline), 2 any AD/census pair,
+// 3 census alone, 4 truncated AD alone (integer costs, u16 segments)
 template <typename ST, int MODE, int GRAYREC>
 __global__ void __launch_bounds__(kHsegW * 32, 8) k_hseg_views(ViewTable t, CostCfg cfg, const float *__restrict__ lut2d) {
     __shared__ __align__(16) float pring[kHsegW][64][32];
@@ -269,6 +270,12 @@ __global__ void __launch_bounds__(kHsegW * 32, 8) k_hseg_views(ViewTable t, Cost
                         s = imin(s, cfg.itrunc);
                         const int hd = __popc(a.x ^ b.x) + __popc(a.y ^ b.y);
                         cv[u] = __ldg(lut2d + s * 65 + hd);
+                    } else if constexpr (MODE == 3) {
+                        // census alone: the Hamming distance (seq/CensusTransform.cpp:39-62)
+                        cv[u] = (float)(__popc(a.x ^ b.x) + __popc(a.y ^ b.y));
+                    } else if constexpr (MODE == 4) {
+                        // truncated AD alone (seq/PixelBasedCost.cpp:13-24, seq/Main.cpp:183-186)
+                        cv[u] = (float)imin((int)__vsadu4(a.z, b.z), cfg.itrunc);
                     } else {
                         cv[u] = pair_cost(a, b, cfg);
                     }
@@ -402,6 +409,37 @@ template <> struct VRing<__half> {
     }
     static __device__ __forceinline__ float sum(Acc a) { return a.s; }
     static __device__ __forceinline__ uint32_t cnt(Acc a) { return a.c & 0xffffu; }
+};
+
+template <> struct VRing<uint16_t> {
+    // integer costs: segment << 12 | row pixel count in one word, and one 32-bit
+    // add accumulates both (a cross's sums stay below 2^20 and its count below
+    // 2^12); the sum is the exact integer the reference's float adds reach
+    using E = uint32_t;
+    using In = unsigned short;
+    struct Acc {
+        uint32_t v;
+    };
+    static __device__ __forceinline__ E make(unsigned short s, uint32_t cnt) { return ((uint32_t)s << 12) | cnt; }
+    static __device__ __forceinline__ Acc zero() { return Acc{0u}; }
+    template <int OFF> static __device__ __forceinline__ E lds(uint32_t a) {
+        E e;
+        asm volatile("ld.shared.u32 %0, [%1+%2];" : "=r"(e) : "r"(a), "n"(OFF));
+        return e;
+    }
+    static __device__ __forceinline__ void add_if_bit(Acc &a, uint32_t m, uint32_t bit, E e) {
+        asm("{\n\t.reg .pred p;\n\t.reg .b32 t;\n\tand.b32 t, %1, %2;\n\tsetp.ne.u32 p, t, 0;\n\t"
+            "@p add.u32 %0, %0, %3;\n\t}"
+            : "+r"(a.v)
+            : "r"(m), "r"(bit), "r"(e));
+    }
+    static __device__ __forceinline__ void add_if_lt(Acc &a, uint32_t x, uint32_t y, E e) {
+        asm("{\n\t.reg .pred p;\n\tsetp.lo.u32 p, %1, %2;\n\t@p add.u32 %0, %0, %3;\n\t}"
+            : "+r"(a.v)
+            : "r"(x), "r"(y), "r"(e));
+    }
+    static __device__ __forceinline__ float sum(Acc a) { return __uint2float_rn(a.v >> 12); }
+    static __device__ __forceinline__ uint32_t cnt(Acc a) { return a.v & 0xfffu; }
 };
 
 // One item (column x, rows y0 .. y1-1) with NC 32-disparity chunks per lane;
@@ -716,6 +754,28 @@ static bool mode1(const rts_params &p) {
 // the largest first-cost value of the table path
 static int mode1_smax(const rts_params &p) { return p.cost1 == RTS_COST_RANK ? 255 : (int)p.ad_trunc; }
 
+// The largest cost of a configuration whose costs are all integers (census
+// alone, or truncated AD alone with an integral truncation), else -1.
+static int int_cost_max(const rts_params &p) {
+    if (p.cost2 != RTS_COST_NONE) return -1;
+    if (p.cost1 == RTS_COST_CENSUS) return (2 * p.census_hrad + 1) * (2 * p.census_wrad + 1);
+    if (p.cost1 == RTS_COST_AD && p.aggr == RTS_AGGR_CROSS && p.ad_trunc >= 0.f && p.ad_trunc <= 765.f &&
+        p.ad_trunc == floorf(p.ad_trunc))
+        return (int)p.ad_trunc;  // seq/Main.cpp:183-186: AD is truncated in the cross-based runs
+    return -1;
+}
+
+int cross_seg_kind(const rts_params &p, int max_w) {
+    const int m = int_cost_max(p);
+    const long cross = (long)(2 * p.cross_arm + 1) * (2 * p.cross_arm + 1);
+    // exact integers all the way: row prefix sums below 2^24 (float), a cross's
+    // sum below 2^20 and its pixel count below 2^12 (the packed vertical adds)
+    if (m >= 0 && cross_record_costs(p) && (long)m * cross < (1L << 20) && cross < 4096 &&
+        (long)max_w * m < (1L << 24))
+        return 2;
+    return p.precision == RTS_PREC_F16 ? 1 : 0;
+}
+
 bool cross_record_costs(const rts_params &p) {
     if (!mode1(p) && !fast_costs(p)) return false;
     const bool census = p.cost1 == RTS_COST_CENSUS || p.cost2 == RTS_COST_CENSUS;
@@ -733,7 +793,7 @@ rts_status cross_tables(rts_ctx *c, const rts_params &p) {
     return RTS_OK;
 }
 
-rts_status launch_cross_views(rts_ctx *c, const rts_params &p, const ViewTable &t, int half, int has_vol, int gray,
+rts_status launch_cross_views(rts_ctx *c, const rts_params &p, const ViewTable &t, int segk, int has_vol, int gray,
                               int max_d, const CrossTune &tune, int *row_last_all, size_t row_last_count) {
     CostCfg cfg;
     cfg.k1 = p.cost1;
@@ -788,7 +848,11 @@ rts_status launch_cross_views(rts_ctx *c, const rts_params &p, const ViewTable &
         StageScope sc(c, "cross_hseg");
         const unsigned g = grid(t.total[ST_HSEG], kHsegW, tune.grid_mult);
         auto go = [&](auto kern) { kern<<<g, kHsegW * 32, 0, s>>>(t, cfg, lut2d); };
-        if (half) {
+        if (segk == 2) {
+            // integer costs: census alone, or truncated AD alone
+            if (p.cost1 == RTS_COST_CENSUS) go(k_hseg_views<uint16_t, 3, 0>);
+            else go(k_hseg_views<uint16_t, 4, 0>);
+        } else if (segk == 1) {
             if (mode == 0) go(k_hseg_views<__half, 0, 0>);
             else if (mode == 1 && grayrec == 2) go(k_hseg_views<__half, 1, 2>);
             else if (mode == 1 && grayrec == 1) go(k_hseg_views<__half, 1, 1>);
@@ -810,7 +874,7 @@ rts_status launch_cross_views(rts_ctx *c, const rts_params &p, const ViewTable &
         const int NCH = nch <= 1 ? 1 : nch <= 2 ? 2 : nch <= 4 ? 4 : 8;
         // ring {segment, count} + arm words + reference arm words + target columns
         const size_t DMb = (size_t)32 * NCH;
-        const size_t smem = (size_t)DEP * DMb * ((half ? 4 : 8) + 2) + (size_t)DEP * 4 + DMb * 4;
+        const size_t smem = (size_t)DEP * DMb * ((segk ? 4 : 8) + 2) + (size_t)DEP * 4 + DMb * 4;
         const int R = tune.vert_rows;
         auto go = [&](auto kern) {
             cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -823,7 +887,12 @@ rts_status launch_cross_views(rts_ctx *c, const rts_params &p, const ViewTable &
         if (mode == 0) go(k_vert_views<ST, N, 0>);        \
         else go(k_vert_views<ST, N, 1>);                  \
     } while (0)
-        if (half) {
+        if (segk == 2) {
+            if (NCH == 1) go(k_vert_views<uint16_t, 1, 1>);
+            else if (NCH == 2) go(k_vert_views<uint16_t, 2, 1>);
+            else if (NCH == 4) go(k_vert_views<uint16_t, 4, 1>);
+            else go(k_vert_views<uint16_t, 8, 1>);
+        } else if (segk == 1) {
             if (NCH == 1) RTS_VERT(__half, 1);
             else if (NCH == 2) RTS_VERT(__half, 2);
             else if (NCH == 4) RTS_VERT(__half, 4);

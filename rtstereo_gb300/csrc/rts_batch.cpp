@@ -22,6 +22,7 @@
 // waits for the device).
 #include <string.h>
 
+#include <algorithm>
 #include <chrono>
 #include <deque>
 #include <map>
@@ -191,10 +192,12 @@ rts_status rts::batch_views_run(rts_ctx *c, int n, const rts_pair *pairs, const 
             (params[0].right_view && (!outs[i].disp_right || !outs[i].mask)))
             return set_error(c, RTS_ERR_INVALID_ARG, "null image or output in the batch");
     const rts_params &p = params[0];
-    const int right = p.right_view ? 1 : 0, half = p.precision == RTS_PREC_F16 ? 1 : 0;
+    const int right = p.right_view ? 1 : 0;
     const int nv = right ? 2 * n : n;
     std::vector<int> W, H, D;
     view_dims(n, pairs, params, right, W, H, D);
+    // segment storage: exact u16 for integer costs, else by the form; half = 2-byte layout
+    const int segk = cross_seg_kind(p, *std::max_element(W.begin(), W.end())), half = segk != 0;
     GraphCache *gc = cache_of(c);
     const std::string key = shape_key(n, pairs, params);
     const size_t bytes = views_bytes(W.data(), H.data(), D.data(), nv, half);
@@ -237,7 +240,7 @@ rts_status rts::batch_views_run(rts_ctx *c, int n, const rts_pair *pairs, const 
             ViewTable t;
             RTS_TRY(upload_views(c, b, cand, nullptr, &t));
             RTS_CU(c, cudaEventRecord(e0, c->stream));
-            RTS_TRY(launch_cross_views(c, p, t, half, 0, gray, b.max_d, cand, b.row_last_all, b.row_last_count));
+            RTS_TRY(launch_cross_views(c, p, t, segk, 0, gray, b.max_d, cand, b.row_last_all, b.row_last_count));
             RTS_CU(c, cudaEventRecord(e1, c->stream));
             RTS_CU(c, cudaEventSynchronize(e1));
             float ms = 0;
@@ -258,7 +261,7 @@ rts_status rts::batch_views_run(rts_ctx *c, int n, const rts_pair *pairs, const 
     RTS_TRY(upload_views(c, b, tune, nullptr, &t));
     if (c->timing) {
         // stage timing wants an event pair around every kernel: launch directly
-        return launch_cross_views(c, p, t, half, 0, gray, b.max_d, tune, b.row_last_all, b.row_last_count);
+        return launch_cross_views(c, p, t, segk, 0, gray, b.max_d, tune, b.row_last_all, b.row_last_count);
     }
     GraphEntry &g = gc->graphs[key];
     if (g.exec && (g.arena != arena || g.arena_bytes != bytes)) {
@@ -273,7 +276,7 @@ rts_status rts::batch_views_run(rts_ctx *c, int n, const rts_pair *pairs, const 
         const uint64_t l0 = c->launches.load();
         cudaGraph_t graph;
         RTS_CU(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-        rts_status st = launch_cross_views(c, p, t, half, 0, gray, b.max_d, tune, b.row_last_all, b.row_last_count);
+        rts_status st = launch_cross_views(c, p, t, segk, 0, gray, b.max_d, tune, b.row_last_all, b.row_last_count);
         cudaError_t ce = cudaStreamEndCapture(c->stream, &graph);
         c->timing = timing;
         if (st != RTS_OK) return st;
@@ -506,7 +509,7 @@ rts_status launch_batch(rts_server *s, std::vector<Request *> &ids) {
     Batch &bt = s->batches[slot];
     const int n = (int)ids.size();
     const rts_params &p = s->base_params;
-    const int right = p.right_view ? 1 : 0, half = p.precision == RTS_PREC_F16 ? 1 : 0;
+    const int right = p.right_view ? 1 : 0;
     std::vector<rts_pair> pairs(n);
     std::vector<rts_params> params(n);
     std::vector<rts_out> outs(n);
@@ -527,6 +530,7 @@ rts_status launch_batch(rts_server *s, std::vector<Request *> &ids) {
     std::vector<int> W, H, D;
     view_dims(n, pairs.data(), params.data(), right, W, H, D);
     const int nv = right ? 2 * n : n;
+    const int segk = cross_seg_kind(p, *std::max_element(W.begin(), W.end())), half = segk != 0;
     int gray = 1;
     for (int i = 0; i < n; i++)
         if (pairs[i].left_rgb && pairs[i].right_rgb) gray = 0;
@@ -563,7 +567,7 @@ rts_status launch_batch(rts_server *s, std::vector<Request *> &ids) {
             tune.vert_rows = 256;
         }
         st = upload_views(c, b, tune, nullptr, &t);
-        if (st == RTS_OK) st = launch_cross_views(c, p, t, half, 0, gray, b.max_d, tune, b.row_last_all, b.row_last_count);
+        if (st == RTS_OK) st = launch_cross_views(c, p, t, segk, 0, gray, b.max_d, tune, b.row_last_all, b.row_last_count);
     }
     for (int i = 0; i < n && st == RTS_OK; i++) {
         Request &r = *ids[i];

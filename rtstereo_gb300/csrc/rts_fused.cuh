@@ -52,6 +52,8 @@ __device__ __forceinline__ float pair_cost(const uint4 &a, const uint4 &b, const
 template <typename T> __device__ __forceinline__ T to_store(float v);
 template <> __device__ __forceinline__ float to_store<float>(float v) { return v; }
 template <> __device__ __forceinline__ __half to_store<__half>(float v) { return __float2half_rn(v); }
+// integer costs: v is an exact non-negative integer below 2^16
+template <> __device__ __forceinline__ uint16_t to_store<uint16_t>(float v) { return (uint16_t)__float2uint_rn(v); }
 __device__ __forceinline__ float to_f32(float v) { return v; }
 __device__ __forceinline__ float to_f32(__half v) { return __half2float(v); }
 

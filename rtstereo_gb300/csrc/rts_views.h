@@ -64,10 +64,15 @@ bool cross_record_costs(const rts_params &p);
 // made before a graph capture so that the launches find them cached.
 rts_status cross_tables(rts_ctx *c, const rts_params &p);
 
+// Row-segment storage of a cross-based launch whose widest view is max_w:
+// 2 exact u16 integers (integer costs, either form), 1 f16 (FP16 form), 0 f32.
+// Layouts (views_bytes, plan_views_at) take `kind != 0` as their 2-byte flag.
+int cross_seg_kind(const rts_params &p, int max_w);
+
 // Launches all stages of the cross-based pipeline over a view table that is
-// already on the device; half selects f16 row segments, gray that no view has
-// an RGB image.
-rts_status launch_cross_views(rts_ctx *c, const rts_params &p, const ViewTable &t, int half, int has_vol, int gray,
+// already on the device; segk is the segment kind (cross_seg_kind, or 0/1 by
+// the form for precomputed volumes), gray that no view has an RGB image.
+rts_status launch_cross_views(rts_ctx *c, const rts_params &p, const ViewTable &t, int segk, int has_vol, int gray,
                               int max_d, const CrossTune &tune, int *row_last_all, size_t row_last_count);
 
 // One batch of views on the device, planned on the host.

@@ -125,6 +125,21 @@ def test_fused_paths_match_oracle(ctx, oracle_mod):
         assert_same(g, o)
 
 
+@pytest.mark.parametrize("c1", [1, 3])
+@pytest.mark.parametrize("prec", [0, 1])
+@pytest.mark.parametrize("W,H,D", [(160, 50, 64), (300, 9, 200), (45, 12, 40)])
+def test_integer_cost_cross_exact_in_both_forms(ctx, oracle_mod, c1, prec, W, H, D):
+    """Census alone or truncated AD alone: the row segments are stored as exact
+    u16 integers and summed as integers, so the FP16 form is bit-exact as well."""
+    import rtstereo_gb300 as R
+    O = oracle_mod
+    L, Rr = synth(W + D + c1, W, H, D, 4, 1)
+    Lc, Rc = np.repeat(L[:, :, None], 3, 2).copy(), np.repeat(Rr[:, :, None], 3, 2).copy()
+    g = ctx.pipeline(R.params(cost1=c1, cost2=0, disp_range=D, precision=prec), L, Rr)
+    o = O.pipeline(O.params(cost1=c1, cost2=0, D=D), L, Rr, Lc, Rc)
+    assert bits_equal(g[0], o[0]) and bits_equal(g[1], o[1]) and bits_equal(g[2], o[2])
+
+
 @pytest.mark.parametrize("W,H,D,rad", [(70, 9, 30, 5), (40, 20, 13, 16), (130, 7, 64, 1), (200, 12, 128, 3),
                                        (72, 40, 66, 16)])
 def test_fused_adaptive_weight_shapes(ctx, oracle_mod, W, H, D, rad):
