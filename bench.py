@@ -681,13 +681,13 @@ def roofline(stages, name, W, H, D, ag, peaks, src, p, ms_pair=None):
     # crossings (written by matching and combining, read by aggregation), the
     # vertical kernel the last two (written by aggregation, read by WTA)
     # integer costs (census or truncated AD alone) keep u16 segments in both forms
-    int_costs = p.cost2 == 0 and (p.cost1 == 3 or (p.cost1 == 1 and float(p.ad_trunc).is_integer()))
+    int_costs = ag == 3 and p.cost2 == 0 and (p.cost1 == 3 or (p.cost1 == 1 and float(p.ad_trunc).is_integer()))
     S = 2 if (p.precision or int_costs) else 4
     views = 2
     byts = views * 2 * S * E
     achieved = byts / (per_launch_ms / 1e3) / 1e9
     peak = peaks["hbm_gbs"]
-    bpe = NCU_BYTES_PER_ENTRY.get((kname, 1 if p.precision else 0))
+    bpe = None if int_costs else NCU_BYTES_PER_ENTRY.get((kname, 1 if p.precision else 0))
     out = {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
            "frac": achieved / peak, "traffic": bpe * views * E if bpe else None, "launches": launches,
            "ms_per_launch": per_launch_ms, "bytes_per_launch": byts, "peak_source": src}

@@ -1,0 +1,53 @@
+"""Host-side helpers of bench.py on CPU: the numpy FP64 adaptive-weight
+reference the FP16 bench line reports against (checked against the oracle's
+FP64 restatement), and the roofline arithmetic of the JSON line."""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+sys.path.insert(0, ROOT)
+
+
+def test_numpy_f64_adaptive_weights_match_oracle(oracle_mod):
+    import bench
+    import rtstereo_gb300 as R
+    O = oracle_mod
+    H, W, D, rad = 30, 48, 12, 16
+    L, Rr, _ = R.synth_pair(9, W, H, D, 3, 0, 2.0, 4)
+    Lc, Rc = R.gray_to_rgb(L), R.gray_to_rgb(Rr)
+    Ll, Rl = R.rgb_to_lab(Lc), R.rgb_to_lab(Rc)
+    rows = [0, 7, 29]
+    got = bench.f64_aw_rows(L, Rr, Lc, Rc, Ll, Rl, D, rad, 7.0, 36.0, 10.0, 10.0, rows, 4, 3)
+    c1 = O.ad_color(Lc, Rc, D)
+    c2 = O.hamming(O.census(L), O.census(Rr), D)
+    want = O.f64_aw_l2r_pre(Ll, Rl, O.f64_combine(c1, c2, 10.0, 10.0), rad, 7.0, 36.0)[rows]
+    assert np.abs(got - want).max() < 1e-12
+
+
+def test_roofline_fields():
+    import bench
+    import rtstereo_gb300 as R
+    peaks = {"hbm_gbs": 6000.0, "sm_max_mhz": 2000.0}
+    # adaptive weights: FP32-pipe bound, 4 ops per tap per entry
+    p = R.params(aggr=2, disp_range=64)
+    r = bench.roofline({"aw_wta": (2, 8.0)}, "aw_640x480_d64", 640, 480, 64, 2, peaks, "measured", p)
+    assert r["bound"] == "fp32" and r["kernel"] == "k_aw_wta_pipe"
+    assert r["ms_per_launch"] == pytest.approx(4.0)
+    assert r["flop_per_launch"] == pytest.approx(4 * 33 * 33 * 640 * 480 * 64)
+    assert r["peak"] == pytest.approx(152 * 128 * 2000e6 / 1e12)
+    assert r["frac"] == pytest.approx(r["achieved"] / r["peak"])
+    # cross-based: HBM stage model, 2 views x 2 crossings x S bytes per entry
+    p = R.params(disp_range=128)
+    stages = {"cross_hseg": (1, 1.0), "cross_vert_wta": (1, 2.0)}
+    r = bench.roofline(stages, "cross_1920x1080_d128", 1920, 1080, 128, 3, peaks, "measured", p, ms_pair=3.5)
+    E = 1920 * 1080 * 128
+    assert r["kernel"] == "cross_vert_wta" and r["bytes_per_launch"] == 2 * 2 * 4 * E
+    assert r["traffic"] == pytest.approx(4.16 * 2 * E)
+    assert r["pipeline"]["bytes_per_pair"] == 2 * (4 * 4 * E) + 2 * (8 * 1920 * 1080) + 3 * 1920 * 1080
+    # integer costs keep 2-byte segments (no ncu traffic figure for them)
+    p = R.params(disp_range=128, cost1=3, cost2=0)
+    r = bench.roofline(stages, "census_cross_1920x1080_d128", 1920, 1080, 128, 3, peaks, "measured", p)
+    assert r["bytes_per_launch"] == 2 * 2 * 2 * E and r["traffic"] is None
