@@ -211,6 +211,10 @@ __global__ void k_ncc(const uint8_t *__restrict__ ref, const uint8_t *__restrict
 //   den term = ((rv*rv)*tv)*tv, (nom, den) += (rv*tv, den term)   (packed add)
 // which are the reference's operations in its order.
 constexpr int kNccTX = 64, kNccTD = 64, kNccTaps = 49;
+// Shared rows hold float2 values in 16-byte chunks; chunk c is stored at
+// c ^ ((c >> 3) & 1), so the eight 16-byte reads of a quarter warp (4 pixels
+// apart) fall in distinct banks.
+__device__ __forceinline__ int ncc_swz(int u) { return (((u >> 1) ^ ((u >> 4) & 1)) << 1) | (u & 1); }
 
 __global__ void __launch_bounds__(256) k_ncc_tiled(const uint8_t *__restrict__ ref, const uint8_t *__restrict__ tar,
                                                    const float *__restrict__ mref, const float *__restrict__ mtar,
@@ -224,6 +228,8 @@ __global__ void __launch_bounds__(256) k_ncc_tiled(const uint8_t *__restrict__ r
     const int y = blockIdx.y, x0 = blockIdx.x * kNccTX, dc0 = blockIdx.z * kNccTD;
     const int tbase = x0 - dc0 - (kNccTD - 1);    // target column of u = 0 (before wrapping)
     const int ew = 2 * wr + 1, taps = (2 * hr + 1) * ew;
+    // the tap offsets {dy, dx} of a chunk, made once per chunk
+    __shared__ int2 tapoff[kNccTaps];
     unsigned long long acc[4][4];  // (nom, den) of pixel px0 + j, disparity d0 + i
 #pragma unroll
     for (int j = 0; j < 4; j++)
@@ -232,39 +238,45 @@ __global__ void __launch_bounds__(256) k_ncc_tiled(const uint8_t *__restrict__ r
     for (int k0 = 0; k0 < taps; k0 += kNccTaps) {
         const int nk = min(kNccTaps, taps - k0);
         __syncthreads();  // the previous chunk is consumed
+        if (tid < nk) {
+            const int kk = k0 + tid, ry = kk / ew;
+            tapoff[tid] = make_int2(ry - hr, kk - ry * ew - wr);
+        }
+        __syncthreads();
         for (int q = tid; q < nk * kNccTX; q += 256) {
             const int k = q / kNccTX, px = q - k * kNccTX;
-            const int kk = k0 + k, dy = kk / ew - hr, dx = kk - (kk / ew) * ew - wr;
+            const int2 to = tapoff[k];
+            const int dy = to.x, dx = to.y;
             const int x = min(x0 + px, W - 1);
             const float mr = mref[(size_t)y * W + x];
             const float rv = __fsub_rn((float)ref[(size_t)wrap1(y + dy, H) * W + wrap1(x + dx, W)], mr);
-            rq[k][px] = make_float2(rv, __fmul_rn(rv, rv));
+            rq[k][ncc_swz(px)] = make_float2(rv, __fmul_rn(rv, rv));
         }
         for (int q = tid; q < nk * NT; q += 256) {
             const int k = q / NT, u = q - k * NT;
-            const int kk = k0 + k, dy = kk / ew - hr, dx = kk - (kk / ew) * ew - wr;
+            const int2 to = tapoff[k];
+            const int dy = to.x, dx = to.y;
             // t in [-W, 2W) for real entries; columns of padding entries clamped into range
             const int t = max(min(tbase + u, W - 1), -W + 1);
             const float mt = mtar[(size_t)y * W + wrap1(t, W)];  // seq/NCCDisparity.cpp:37-48, same columns
             const float tv = __fsub_rn((float)tar[(size_t)wrap1(y + dy, H) * W + wrap1(wrap1(t, W) + dx, W)], mt);
-            tq[k][u] = make_float2(tv, tv);
+            tq[k][ncc_swz(u)] = make_float2(tv, tv);
         }
         __syncthreads();
         // u index of (j, i): px0 + j - d0 - i + 63
         const int ub = px0 - d0 + kNccTD - 4;
 #pragma unroll 1
         for (int k = 0; k < nk; k++) {
-            unsigned long long r[4], tt[7];
-            const ulonglong2 ra = *reinterpret_cast<const ulonglong2 *>(&rq[k][px0]);
-            const ulonglong2 rb = *reinterpret_cast<const ulonglong2 *>(&rq[k][px0 + 2]);
+            unsigned long long r[4], tt[8];
+            const ulonglong2 ra = *reinterpret_cast<const ulonglong2 *>(&rq[k][ncc_swz(px0)]);
+            const ulonglong2 rb = *reinterpret_cast<const ulonglong2 *>(&rq[k][ncc_swz(px0 + 2)]);
             r[0] = ra.x; r[1] = ra.y; r[2] = rb.x; r[3] = rb.y;
 #pragma unroll
-            for (int m = 0; m < 3; m++) {
-                const ulonglong2 v = *reinterpret_cast<const ulonglong2 *>(&tq[k][ub + 2 * m]);
+            for (int m = 0; m < 4; m++) {
+                const ulonglong2 v = *reinterpret_cast<const ulonglong2 *>(&tq[k][ncc_swz(ub + 2 * m)]);
                 tt[2 * m] = v.x;
                 tt[2 * m + 1] = v.y;
             }
-            tt[6] = *reinterpret_cast<const unsigned long long *>(&tq[k][ub + 6]);
 #pragma unroll
             for (int j = 0; j < 4; j++)
 #pragma unroll
