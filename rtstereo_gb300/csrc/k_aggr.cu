@@ -81,20 +81,35 @@ __global__ void __launch_bounds__(256) k_box_best(const float *__restrict__ vol,
     if (y >= H) return;
 #pragma unroll 1
     for (int g = 0; g < kBoxTX / G; g++) {
-        float sm[G];
+        // the chains of pixels (2m, 2m + 1) advance together on packed f32x2 adds
+        // (each half the reference's own add, in its order)
+        unsigned long long sp[G / 2];
 #pragma unroll
-        for (int j = 0; j < G; j++) sm[j] = 0.f;
+        for (int m = 0; m < G / 2; m++) sp[m] = 0ull;
 #pragma unroll
         for (int dy = 0; dy <= 2 * R; dy++) {
-            float v[G + 2 * R];
+            constexpr int NV = G + 2 * R;  // even
+            float v[NV];
             const float *rp = bt + ((warp + dy) * TW + G * g) * 32 + lane;
 #pragma unroll
-            for (int k = 0; k < G + 2 * R; k++) v[k] = rp[k * 32];
+            for (int k = 0; k < NV; k++) v[k] = rp[k * 32];
+            // {v[k], v[k + 1]} for even k (pe) and odd k (po)
+            unsigned long long pe[NV / 2], po[NV / 2 - 1];
 #pragma unroll
-            for (int j = 0; j < G; j++)
+            for (int i = 0; i < NV / 2; i++) pe[i] = pack2(v[2 * i], v[2 * i + 1]);
 #pragma unroll
-                for (int dx = 0; dx <= 2 * R; dx++) sm[j] = __fadd_rn(sm[j], v[j + dx]);
+            for (int i = 0; i < NV / 2 - 1; i++) po[i] = pack2(v[2 * i + 1], v[2 * i + 2]);
+#pragma unroll
+            for (int m = 0; m < G / 2; m++)
+#pragma unroll
+                for (int dx = 0; dx <= 2 * R; dx++) {
+                    const int k = 2 * m + dx;
+                    sp[m] = add2(sp[m], (k & 1) ? po[(k - 1) / 2] : pe[k / 2]);
+                }
         }
+        float sm[G];
+#pragma unroll
+        for (int j = 0; j < G; j++) sm[j] = half2_of(sp[j / 2], j & 1);
 #pragma unroll
         for (int j = 0; j < G; j++) {
             const int x = x0 + G * g + j;
