@@ -299,6 +299,42 @@ __global__ void __launch_bounds__(256) k_ncc_tiled(const uint8_t *__restrict__ r
         }
 }
 
+// LoG differences combined with census Hamming distances in one pass (the
+// composed k_ad_1ch<float> + k_hamming + k_combine of seq/Main.cpp:180-234 with
+// LoG first and census second): the same expressions in the same order, one
+// write of the volume.  A warp takes kLcPx consecutive pixels, lane = disparity.
+constexpr int kLcPx = 8;
+
+template <int NW>
+__global__ void __launch_bounds__(256) k_cost_log_census(const float *__restrict__ lr, const float *__restrict__ lt,
+                                                        const uint64_t *__restrict__ cr, const uint64_t *__restrict__ ct,
+                                                        float *__restrict__ vol, int H, int W, int D,
+                                                        const float *__restrict__ lut1, const float *__restrict__ lut2,
+                                                        float lambda1, float lambda2) {
+    const int y = blockIdx.y, lane = threadIdx.x & 31;
+    const int xw = (blockIdx.x * 8 + (threadIdx.x >> 5)) * kLcPx;
+    const size_t row = (size_t)y * W;
+#pragma unroll 2
+    for (int i = 0; i < kLcPx; i++) {
+        const int x = xw + i;
+        if (x >= W) return;
+        const float a = lr[row + x];
+        uint64_t ca[NW];
+#pragma unroll
+        for (int j = 0; j < NW; j++) ca[j] = cr[(row + x) * NW + j];
+        float *out = vol + (row + x) * D;
+        for (int d = lane; d < D; d += 32) {
+            const int xt = x - d < 0 ? x - d + W : x - d;  // seq/PixelBasedCost.cpp:19-20
+            float v1 = __fsub_rn(a, lt[row + xt]);         // seq/PixelBasedCost.cpp:48-50
+            if (v1 < 0) v1 = -v1;
+            int cnt = 0;
+#pragma unroll
+            for (int j = 0; j < NW; j++) cnt += __popcll(ca[j] ^ ct[(row + xt) * NW + j]);  // seq/CensusTransform.cpp:60
+            out[d] = __fadd_rn(combine_term(v1, lut1, lambda1), combine_term((float)cnt, lut2, lambda2));
+        }
+    }
+}
+
 __global__ void k_combine(float *__restrict__ c1, const float *__restrict__ c2, long n, const float *__restrict__ lut1,
                           const float *__restrict__ lut2, float lambda1, float lambda2) {
     for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
@@ -366,6 +402,14 @@ void launch_ncc(cudaStream_t s, const uint8_t *ref, const uint8_t *tar, const fl
     const size_t smem = sizeof(float2) * kNccTaps * (kNccTX + kNccTX + kNccTD);
     cudaFuncSetAttribute(k_ncc_tiled, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     k_ncc_tiled<<<g, 256, smem, s>>>(ref, tar, mref, mtar, cost, D, H, W, hr, wr);
+}
+void launch_cost_log_census(cudaStream_t s, const float *lr, const float *lt, const uint64_t *cr, const uint64_t *ct,
+                            int nw, float *vol, int D, int H, int W, const float *lut1, const float *lut2,
+                            float lambda1, float lambda2) {
+    const dim3 g((unsigned)((W + 8 * kLcPx - 1) / (8 * kLcPx)), H);
+    if (nw == 1) k_cost_log_census<1><<<g, 256, 0, s>>>(lr, lt, cr, ct, vol, H, W, D, lut1, lut2, lambda1, lambda2);
+    else if (nw == 2) k_cost_log_census<2><<<g, 256, 0, s>>>(lr, lt, cr, ct, vol, H, W, D, lut1, lut2, lambda1, lambda2);
+    else k_cost_log_census<4><<<g, 256, 0, s>>>(lr, lt, cr, ct, vol, H, W, D, lut1, lut2, lambda1, lambda2);
 }
 void launch_combine(cudaStream_t s, float *c1, const float *c2, long n, const float *lut1, const float *lut2,
                     float lambda1, float lambda2) {

@@ -157,6 +157,10 @@ void launch_convolve(cudaStream_t s, const uint8_t *img, float *out, const float
 void launch_window_mean(cudaStream_t s, const uint8_t *img, float *mean, int H, int W, int hr, int wr);
 void launch_ncc(cudaStream_t s, const uint8_t *ref, const uint8_t *tar, const float *mref, const float *mtar,
                 float *cost, int D, int H, int W, int hr, int wr);
+// LoG first cost combined with census second cost in one pass (nw census words)
+void launch_cost_log_census(cudaStream_t s, const float *lr, const float *lt, const uint64_t *cr, const uint64_t *ct,
+                            int nw, float *vol, int D, int H, int W, const float *lut1, const float *lut2,
+                            float lambda1, float lambda2);
 void launch_combine(cudaStream_t s, float *c1, const float *c2, long n, const float *lut1, const float *lut2,
                     float lambda1, float lambda2);
 // k_aggr.cu

@@ -126,6 +126,28 @@ static rts_status one_cost(rts_ctx *c, const rts_params &p, int which, bool trun
 // cost1 (and cost2 combined, seq/Main.cpp:180-234) into `out` with the module kernels
 static rts_status cost_volume_composed(rts_ctx *c, const rts_params &p, int H, int W, const ViewIn &v, float *out) {
     const size_t ne = (size_t)H * W * p.disp_range;
+    const int nw = census_words(p.census_hrad, p.census_wrad);
+    if (p.cost1 == RTS_COST_LOG && p.cost2 == RTS_COST_CENSUS && nw > 0) {
+        // LoG and census terms combined as the volume is written (one pass)
+        const size_t np = (size_t)H * W;
+        cudaStream_t s = c->stream;
+        void *aux, *mask, *codes;
+        RTS_TRY(scratch(c, SL_V_AUX, np * 8, &aux));
+        RTS_TRY(scratch(c, SL_TMP3, sizeof(kLog5x5), &mask));
+        RTS_TRY(scratch(c, SL_V_CODES, np * nw * 16, &codes));
+        RTS_CU(c, cudaMemcpyAsync(mask, kLog5x5, sizeof(kLog5x5), cudaMemcpyHostToDevice, s));
+        float *la = (float *)aux, *lb = la + np;
+        uint64_t *ca = (uint64_t *)codes, *cb = ca + np * nw;
+        launch_convolve(s, v.gref, la, (const float *)mask, H, W, 2, 2);
+        launch_convolve(s, v.gtar, lb, (const float *)mask, H, W, 2, 2);
+        launch_census_codes(s, v.gref, ca, p.census_hrad, p.census_wrad, H, W);
+        launch_census_codes(s, v.gtar, cb, p.census_hrad, p.census_wrad, H, W);
+        const float *l1, *l2;
+        RTS_TRY(combine_luts(c, p.lambda1, p.lambda2, &l1, &l2));
+        launch_cost_log_census(s, la, lb, ca, cb, nw, out, p.disp_range, H, W, l1, l2, p.lambda1, p.lambda2);
+        count_launch(c, 5);
+        return RTS_OK;
+    }
     RTS_TRY(one_cost(c, p, p.cost1, p.aggr == RTS_AGGR_CROSS, H, W, v, out, SL_V_AUX));
     if (p.cost2 != RTS_COST_NONE) {
         void *c2v;

@@ -125,6 +125,25 @@ def test_fused_paths_match_oracle(ctx, oracle_mod):
         assert_same(g, o)
 
 
+@pytest.mark.parametrize("W,H,D", [(96, 40, 32), (200, 13, 130)])
+def test_fused_log_census_volume_equals_modules(ctx, W, H, D):
+    """The one-pass LoG + census volume is the composed modules' volume bit for
+    bit (convolveImage, pixelBasedCostL2R_Float, census + Hamming, combineCost)."""
+    import rtstereo_gb300 as R
+    L, Rr = synth(W * 3 + D, W, H, D, 4)
+    p = R.params(cost1=4, cost2=3, aggr=3, disp_range=D, right_view=0)
+    got = ctx.pipeline(p, L, Rr, want_cost=True)
+    c1 = ctx.pixelBasedCostL2R_Float(ctx.convolveImage(L), ctx.convolveImage(Rr), D)
+    c2 = ctx.calcHammingDist(ctx.calcCensusTrans(L), ctx.calcCensusTrans(Rr), D)
+    cc = ctx.combineCost(c1, c2, 10.0, 10.0)
+    # the pipeline's returned volume is the aggregated one; compare the costs through
+    # the modules' aggregation of the same volume
+    h, v = ctx.findCross(R.gray_to_rgb(L))
+    ht, vt = ctx.findCross(R.gray_to_rgb(Rr))
+    agg = ctx.cross_stereo_aggregation(ctx.aggregate_cost_horizontal(cc), h, ht, v, vt)
+    assert bits_equal(got[3], agg)
+
+
 @pytest.mark.parametrize("c1", [1, 3])
 @pytest.mark.parametrize("prec", [0, 1])
 @pytest.mark.parametrize("W,H,D", [(160, 50, 64), (300, 9, 200), (45, 12, 40)])
