@@ -30,9 +30,16 @@ __global__ void k_prep_records(const uint8_t *__restrict__ gray, const uint8_t *
         // seq/CensusTransform.cpp:11-37, bit (dy+hr)*(2wr+1)+(dx+wr), strict centre > neighbour
         const uint8_t c = gray[p];
         int k = 0;
-        for (int dy = -hr; dy <= hr; dy++) {
-            const uint8_t *row = gray + (size_t)wrap1(y + dy, H) * W;
-            for (int dx = -wr; dx <= wr; dx++, k++) code |= (uint64_t)(c > row[wrap1(x + dx, W)]) << k;
+        if (x >= wr && x < W - wr && y >= hr && y < H - hr) {
+            // the window inside the image: no wrapping
+            const uint8_t *row = gray + p - (size_t)hr * W - wr;
+            for (int dy = -hr; dy <= hr; dy++, row += W)
+                for (int dx = 0; dx <= 2 * wr; dx++, k++) code |= (uint64_t)(c > row[dx]) << k;
+        } else {
+            for (int dy = -hr; dy <= hr; dy++) {
+                const uint8_t *row = gray + (size_t)wrap1(y + dy, H) * W;
+                for (int dx = -wr; dx <= wr; dx++, k++) code |= (uint64_t)(c > row[wrap1(x + dx, W)]) << k;
+            }
         }
     }
     const uint8_t *px = rgb + 3 * p;
