@@ -82,13 +82,20 @@ __global__ void k_census_codes(const uint8_t *__restrict__ img, uint64_t *__rest
 #pragma unroll
     for (int j = 0; j < NW; j++) w[j] = 0;
     int k = 0;
-    for (int dy = -hr; dy <= hr; dy++) {
-        const uint8_t *row = img + (size_t)wrap1(y + dy, H) * W;
-        for (int dx = -wr; dx <= wr; dx++, k++) {
-            const uint64_t bit = (c > row[wrap1(x + dx, W)]) ? 1ull : 0ull;
+    if (NW == 1 && x >= wr && x < W - wr && y >= hr && y < H - hr) {
+        // the window inside the image: no wrapping
+        const uint8_t *row = img + (size_t)(y - hr) * W + x - wr;
+        for (int dy = -hr; dy <= hr; dy++, row += W)
+            for (int dx = 0; dx <= 2 * wr; dx++, k++) w[0] |= (uint64_t)(c > row[dx]) << k;
+    } else {
+        for (int dy = -hr; dy <= hr; dy++) {
+            const uint8_t *row = img + (size_t)wrap1(y + dy, H) * W;
+            for (int dx = -wr; dx <= wr; dx++, k++) {
+                const uint64_t bit = (c > row[wrap1(x + dx, W)]) ? 1ull : 0ull;
 #pragma unroll
-            for (int j = 0; j < NW; j++)
-                if ((k >> 6) == j) w[j] |= bit << (k & 63);
+                for (int j = 0; j < NW; j++)
+                    if ((k >> 6) == j) w[j] |= bit << (k & 63);
+            }
         }
     }
 #pragma unroll
@@ -152,10 +159,19 @@ __global__ void k_convolve(const uint8_t *__restrict__ img, float *__restrict__ 
     if (x >= W) return;
     const int mw = 2 * wr + 1;
     float acc = 0.f;
-    for (int dy = -hr; dy <= hr; dy++) {
-        const uint8_t *row = img + (size_t)wrap1(y + dy, H) * W;
-        const float *mk = mask + (dy + hr) * mw + wr;
-        for (int dx = -wr; dx <= wr; dx++) acc = __fadd_rn(acc, __fmul_rn((float)row[wrap1(x + dx, W)], mk[dx]));
+    if (x >= wr && x < W - wr && y >= hr && y < H - hr) {
+        // the window inside the image: no wrapping (same products, same order)
+        const uint8_t *row = img + (size_t)(y - hr) * W + x;
+        for (int dy = -hr; dy <= hr; dy++, row += W) {
+            const float *mk = mask + (dy + hr) * mw + wr;
+            for (int dx = -wr; dx <= wr; dx++) acc = __fadd_rn(acc, __fmul_rn((float)row[dx], mk[dx]));
+        }
+    } else {
+        for (int dy = -hr; dy <= hr; dy++) {
+            const uint8_t *row = img + (size_t)wrap1(y + dy, H) * W;
+            const float *mk = mask + (dy + hr) * mw + wr;
+            for (int dx = -wr; dx <= wr; dx++) acc = __fadd_rn(acc, __fmul_rn((float)row[wrap1(x + dx, W)], mk[dx]));
+        }
     }
     acc = (acc > 0.f) ? acc : -acc;
     out[(size_t)y * W + x] = (acc > 255.f) ? 255.f : acc;
