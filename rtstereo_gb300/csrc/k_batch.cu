@@ -881,10 +881,13 @@ rts_status launch_cross_views(rts_ctx *c, const rts_params &p, const ViewTable &
             kern<<<grid(t.total[ST_VERT], 1, resident_blocks(kern, kVertT, smem)), kVertT, smem, s>>>(t, L, R, DEP,
                                                                                                    rcp);
         };
-        // non-negative costs (every cost computed from records) take the fast exact division
+        // non-negative costs take the fast exact division: every cost made from records,
+        // and every precomputed volume but NCC's (AD, rank and LoG differences, Hamming
+        // distances and their CombineCost terms 1 - exp(-v / lambda) are >= 0)
+        const bool pos = mode != 0 || (p.cost1 != RTS_COST_NCC && p.cost2 != RTS_COST_NCC);
 #define RTS_VERT(ST, N)                                   \
     do {                                                  \
-        if (mode == 0) go(k_vert_views<ST, N, 0>);        \
+        if (!pos) go(k_vert_views<ST, N, 0>);             \
         else go(k_vert_views<ST, N, 1>);                  \
     } while (0)
         if (segk == 2) {

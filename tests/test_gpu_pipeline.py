@@ -144,6 +144,19 @@ def test_fused_log_census_volume_equals_modules(ctx, W, H, D):
     assert bits_equal(got[3], agg)
 
 
+@pytest.mark.parametrize("c1,c2", [(4, 3), (4, 0), (2, 0)])
+def test_volume_views_equal_composed_modules(ctx, c1, c2):
+    """Cross-based views over a precomputed volume (LoG, rank alone) give the
+    disparities of the composed module path on the same volume."""
+    import rtstereo_gb300 as R
+    L, Rr = synth(c1 * 10 + c2, 160, 48, 48, 5, 1)
+    p = R.params(cost1=c1, cost2=c2, aggr=3, disp_range=48, rank_rad=3)
+    views = ctx.pipeline(p, L, Rr)
+    composed = ctx.pipeline(p, L, Rr, want_cost=True)
+    for a, b in zip(views[:3], composed[:3]):
+        assert bits_equal(a, b)
+
+
 @pytest.mark.parametrize("c1", [1, 3])
 @pytest.mark.parametrize("prec", [0, 1])
 @pytest.mark.parametrize("W,H,D", [(160, 50, 64), (300, 9, 200), (45, 12, 40)])
