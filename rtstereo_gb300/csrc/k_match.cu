@@ -193,32 +193,8 @@ __global__ void k_window_mean(const uint8_t *__restrict__ img, float *__restrict
     mean[(size_t)y * W + x] = __fdiv_rn(s, (float)((2 * hr + 1) * (2 * wr + 1)));
 }
 
-// NCC (seq/NCCDisparity.cpp:50-71): nom = sum rv*tv, den = sqrtf(sum ((rv*rv)*tv)*tv);
-// the cell is written only when den != 0.
-__global__ void k_ncc(const uint8_t *__restrict__ ref, const uint8_t *__restrict__ tar,
-                      const float *__restrict__ mref, const float *__restrict__ mtar, float *__restrict__ cost,
-                      int D, int H, int W, int hr, int wr) {
-    const int y = blockIdx.y;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= W * D) return;
-    const int x = i / D, d = i - x * D;
-    const float mr = mref[(size_t)y * W + x];
-    const float mt = mtar[(size_t)y * W + wrap1(x - d, W)];
-    float nom = 0.f, den = 0.f;
-    for (int dy = -hr; dy <= hr; dy++) {
-        const size_t row = (size_t)wrap1(y + dy, H) * W;
-        for (int dx = -wr; dx <= wr; dx++) {
-            const float rv = __fsub_rn((float)ref[row + wrap1(x + dx, W)], mr);
-            const float tv = __fsub_rn((float)tar[row + wrap1(x + dx - d, W)], mt);
-            nom = __fadd_rn(nom, __fmul_rn(rv, tv));
-            den = __fadd_rn(den, __fmul_rn(__fmul_rn(__fmul_rn(rv, rv), tv), tv));
-        }
-    }
-    den = __fsqrt_rn(den);
-    if (den != 0.f) cost[((size_t)y * W + x) * D + d] = __fdiv_rn(nom, den);
-}
-
-// NCC over tiles (the same arithmetic as k_ncc): block per (row y, 64 pixels,
+// NCC (seq/NCCDisparity.cpp:50-71): nom = sum rv*tv, den = sqrtf(sum ((rv*rv)*tv)*tv)
+// in tap (raster) order, the cell written only when den != 0.  Over tiles: block per (row y, 64 pixels,
 // 64 disparities), each thread 4 pixels x 4 disparities.  Per chunk of taps the
 // block stages, in tap (raster) order, {rv, rv*rv} of its 64 reference pixels and
 // {tv, tv} of the 127 target columns t = x - d it meets (rv = I - mean, tv likewise,
