@@ -235,24 +235,29 @@ __global__ void __launch_bounds__(256) k_ncc_tiled(const uint8_t *__restrict__ r
             tapoff[tid] = make_int2(ry - hr, kk - ry * ew - wr);
         }
         __syncthreads();
-        for (int q = tid; q < nk * kNccTX; q += 256) {
-            const int k = q / kNccTX, px = q - k * kNccTX;
-            const int2 to = tapoff[k];
-            const int dy = to.x, dx = to.y;
+        {
+            // reference cells: a thread keeps one pixel (its mean loaded once) over every
+            // 4th tap of the chunk
+            const int px = tid & (kNccTX - 1);
             const int x = min(x0 + px, W - 1);
             const float mr = mref[(size_t)y * W + x];
-            const float rv = __fsub_rn((float)ref[(size_t)wrap1(y + dy, H) * W + wrap1(x + dx, W)], mr);
-            rq[k][ncc_swz(px)] = make_float2(rv, __fmul_rn(rv, rv));
+            for (int k = tid >> 6; k < nk; k += 256 / kNccTX) {
+                const int2 to = tapoff[k];
+                const float rv = __fsub_rn((float)ref[(size_t)wrap1(y + to.x, H) * W + wrap1(x + to.y, W)], mr);
+                rq[k][ncc_swz(px)] = make_float2(rv, __fmul_rn(rv, rv));
+            }
         }
-        for (int q = tid; q < nk * NT; q += 256) {
-            const int k = q / NT, u = q - k * NT;
-            const int2 to = tapoff[k];
-            const int dy = to.x, dx = to.y;
+        if (tid < 2 * NT) {
+            // target cells: threads 0 .. 2 NT - 1 keep one column each over every other tap
+            const int u = tid < NT ? tid : tid - NT;
             // t in [-W, 2W) for real entries; columns of padding entries clamped into range
-            const int t = max(min(tbase + u, W - 1), -W + 1);
-            const float mt = mtar[(size_t)y * W + wrap1(t, W)];  // seq/NCCDisparity.cpp:37-48, same columns
-            const float tv = __fsub_rn((float)tar[(size_t)wrap1(y + dy, H) * W + wrap1(wrap1(t, W) + dx, W)], mt);
-            tq[k][ncc_swz(u)] = make_float2(tv, tv);
+            const int t = wrap1(max(min(tbase + u, W - 1), -W + 1), W);
+            const float mt = mtar[(size_t)y * W + t];  // seq/NCCDisparity.cpp:37-48, same columns
+            for (int k = tid < NT ? 0 : 1; k < nk; k += 2) {
+                const int2 to = tapoff[k];
+                const float tv = __fsub_rn((float)tar[(size_t)wrap1(y + to.x, H) * W + wrap1(t + to.y, W)], mt);
+                tq[k][ncc_swz(u)] = make_float2(tv, tv);
+            }
         }
         __syncthreads();
         // u index of (j, i): px0 + j - d0 - i + 63
