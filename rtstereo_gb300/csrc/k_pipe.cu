@@ -12,6 +12,8 @@
 //   k_aw_wta        adaptive-weight aggregation (seq/AdaptiveWeightAggregation.cpp:73-111)
 //                   over 64-pixel x 64-disparity tiles, weights made on the fly from
 //                   Lab + host tables, and the arg-min over d
+#include <algorithm>
+
 #include "rts_fused.cuh"
 #include "rts_pipe.h"
 
@@ -126,6 +128,7 @@ __global__ void __launch_bounds__(256) k_cost_volume_adc(const uint4 *__restrict
 // product of the byte-wise absolute differences of the packed Lab words.
 constexpr int kAwTX = 64, kAwDC = 64, kAwThreads = 256;
 constexpr int kAwCPitch = kAwDC + 4;
+constexpr int kAwHPitch = kAwDC + 8;  // f16 cost rows: 144 bytes, a multiple of 16
 constexpr uint32_t kLabOut = 0xff000000u;  // marks a column outside the image
 
 __global__ void k_pack_lab(const uint8_t *__restrict__ lab, uint32_t *__restrict__ out, long n) {
@@ -377,14 +380,15 @@ __global__ void __launch_bounds__(kAwThreads, 3) k_aw_wta(const CT *__restrict__
 }
 
 // ---------------------------------------------------------------------------
-// The plain form of k_aw_wta, software-pipelined over the tap rows: while the
+// k_aw_wta, software-pipelined over the tap rows: while the
 // block adds tap row ky, the cost rows of ky + 1 arrive by cp.async in the
 // other buffer, the weights of ky + 1 are made in slices between the groups of
 // taps (their table reads in flight across a group), and the Lab rows of
 // ky + 2 are staged; one barrier per tap row.  The arithmetic per entry is
-// k_aw_wta's (the reference's order, unfused), so the results are the same.
-template <int DUMMY>
-__global__ void __launch_bounds__(kAwThreads, 2) k_aw_wta_pipe(const float *__restrict__ vol,
+// k_aw_wta's: EXACT (plain form, f32 volume) the reference's order, unfused;
+// otherwise (FP16 form, f16 volume staged as f16, D a multiple of 8) one FMA.
+template <typename CT, bool EXACT>
+__global__ void __launch_bounds__(kAwThreads, 2) k_aw_wta_pipe(const CT *__restrict__ vol,
                                                           const uint32_t *__restrict__ labr,
                                                           const uint32_t *__restrict__ labt,
                                                           const float *__restrict__ pw, const float *__restrict__ G,
@@ -393,7 +397,9 @@ __global__ void __launch_bounds__(kAwThreads, 2) k_aw_wta_pipe(const float *__re
     const int r = e >> 1;
     constexpr int NT = kAwTX + kAwDC - 1;  // target columns of a tile
     constexpr int NTP = NT + 1;
-    const int CS = (kAwTX + 2 * r + 4) * kAwCPitch;  // floats of one cost buffer
+    // cost rows: kAwCPitch floats, or kAwHPitch halves (16-byte rows for the copies)
+    constexpr int CP = sizeof(CT) == 4 ? kAwCPitch : kAwHPitch;
+    const int CS = (kAwTX + 2 * r + 4) * CP * (int)sizeof(CT) / 4;  // floats of one cost buffer
     extern __shared__ __align__(16) float asm_[];
     // buffer b: costs at asm_ + b CS, reference weights at wR0 + b e 64, target weights at wT0 + b e NTP
     float *const wR0 = asm_ + 2 * CS, *const wT0 = wR0 + 2 * e * kAwTX;
@@ -440,7 +446,19 @@ __global__ void __launch_bounds__(kAwThreads, 2) k_aw_wta_pipe(const float *__re
         auto stage_cost = [&](int ky, float *C) {
             const size_t crow = (size_t)(y + ky) * W;
             const uint32_t cbase = (uint32_t)__cvta_generic_to_shared(C);
-            if (vec) {
+            if constexpr (sizeof(CT) == 2) {
+                // f16 volume: 16-byte copies of 8 disparities (D is a multiple of 8)
+                for (int q = tid; q < (kAwTX + 2 * r) * (kAwDC / 8); q += kAwThreads) {
+                    const int xi = q >> 3, d8 = (q & 7) * 8;
+                    const int xs = imin(imax(wrap1(x0 - r + xi, W), 0), W - 1);
+                    const int dg = dc0 + d8;
+                    const CT *src = vol + (crow + xs) * D + (dg < D ? dg : 0);
+                    const uint32_t dst = cbase + (uint32_t)((xi * CP + d8) * 2);
+                    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(dst), "l"(src),
+                                 "r"(dg < D ? 16 : 0)
+                                 : "memory");
+                }
+            } else if (vec) {
                 for (int q = tid; q < (kAwTX + 2 * r) * (kAwDC / 4); q += kAwThreads) {
                     const int xi = q >> 4, d4 = (q & 15) * 4;
                     const int xs = imin(imax(wrap1(x0 - r + xi, W), 0), W - 1);
@@ -547,9 +565,21 @@ __global__ void __launch_bounds__(kAwThreads, 2) k_aw_wta_pipe(const float *__re
             float *wRn = wR0 + (b ^ 1) * e * kAwTX, *wTn = wT0 + (b ^ 1) * e * NTP;
 
             const int ubase = px0 - 4 * td + kAwDC - 4;
-            const float *cp = Cs + px0 * kAwCPitch + 4 * td;
+            const CT *cp = reinterpret_cast<const CT *>(Cs) + px0 * CP + 4 * td;
             const float *wrp = wRs + px0;
             const float *wtp = wTs + ubase;
+            // four disparities of a staged cost column as floats
+            auto col4 = [&](const CT *q, float *o) {
+                if constexpr (sizeof(CT) == 4) {
+                    const float4 v = *reinterpret_cast<const float4 *>(q);
+                    o[0] = v.x; o[1] = v.y; o[2] = v.z; o[3] = v.w;
+                } else {
+                    const uint2 hv = *reinterpret_cast<const uint2 *>(q);
+                    const float2 f0 = __half22float2(*reinterpret_cast<const __half2 *>(&hv.x));
+                    const float2 f1 = __half22float2(*reinterpret_cast<const __half2 *>(&hv.y));
+                    o[0] = f0.x; o[1] = f0.y; o[2] = f1.x; o[3] = f1.y;
+                }
+            };
             auto tap = [&](const float (*cw)[4], int cofs, const float *wr4, const float *wt7) {
                 float wr[4], wt[7];
                 const float4 a0 = *reinterpret_cast<const float4 *>(wr4);
@@ -566,12 +596,13 @@ __global__ void __launch_bounds__(kAwThreads, 2) k_aw_wta_pipe(const float *__re
                                                            __fmul_rn(wr[j], wt[j - 2 * h + 2]));
                         const unsigned long long c = pack2(cw[j + cofs][2 * h], cw[j + cofs][2 * h + 1]);
                         sw[j][h] = add2(sw[j][h], w);
-                        sc[j][h] = add2(sc[j][h], mul2(c, w));
+                        if constexpr (EXACT) sc[j][h] = add2(sc[j][h], mul2(c, w));
+                        else sc[j][h] = fma2(c, w, sc[j][h]);
                     }
             };
             int kx = 0, sj = 0;
 #pragma unroll 1
-            for (; kx + 4 <= e; kx += 4, cp += 4 * kAwCPitch, wrp += 4 * kAwTX, wtp += 4 * NTP, sj++) {
+            for (; kx + 4 <= e; kx += 4, cp += 4 * CP, wrp += 4 * kAwTX, wtp += 4 * NTP, sj++) {
                 // a slice of the next tap row's weights around this group of taps
                 const int ks = warp + NW * sj;
                 const bool dos = next && ks < e;
@@ -579,22 +610,16 @@ __global__ void __launch_bounds__(kAwThreads, 2) k_aw_wta_pipe(const float *__re
                 if (dos) slice_issue(sl, ky + 1, ks, lnext);
                 float cw[7][4];
 #pragma unroll
-                for (int q = 0; q < 7; q++) {
-                    const float4 v = *reinterpret_cast<const float4 *>(cp + q * kAwCPitch);
-                    cw[q][0] = v.x; cw[q][1] = v.y; cw[q][2] = v.z; cw[q][3] = v.w;
-                }
+                for (int q = 0; q < 7; q++) col4(cp + q * CP, cw[q]);
 #pragma unroll
                 for (int u = 0; u < 4; u++) tap(cw, u, wrp + u * kAwTX, wtp + u * NTP);
                 if (dos) slice_finish(sl, ky + 1, ks, wRn, wTn);
             }
 #pragma unroll 1
-            for (; kx < e; kx++, cp += kAwCPitch, wrp += kAwTX, wtp += NTP) {
+            for (; kx < e; kx++, cp += CP, wrp += kAwTX, wtp += NTP) {
                 float cw[4][4];
 #pragma unroll
-                for (int q = 0; q < 4; q++) {
-                    const float4 v = *reinterpret_cast<const float4 *>(cp + q * kAwCPitch);
-                    cw[q][0] = v.x; cw[q][1] = v.y; cw[q][2] = v.z; cw[q][3] = v.w;
-                }
+                for (int q = 0; q < 4; q++) col4(cp + q * CP, cw[q]);
                 tap(cw, 0, wrp, wtp);
             }
             // slices the groups did not reach (short windows)
@@ -739,15 +764,27 @@ rts_status aw_fused(rts_ctx *c, const rts_params &p, int H, int W, const void *v
     };
     // plain form: bit-exact float volume, the pipelined kernel; FP16 form: __half
     // volume and fused multiply-add
-    if (half) {
+    // the pipelined kernel: two cost buffers (f32 rows, or f16 rows of 8-disparity
+    // copies; their space also holds the [64][65] argmin staging), two weight
+    // buffers, three Lab row pairs
+    auto pipe_smem = [&](size_t row_bytes) {
+        const size_t costs = 2 * (size_t)(kAwTX + 2 * r + 4) * row_bytes;
+        return std::max(costs, (size_t)kAwTX * (kAwDC + 1) * 4) +
+               sizeof(float) * (2 * (size_t)e * kAwTX + 2 * (size_t)e * (kAwTX + kAwDC)) +
+               sizeof(uint32_t) * 3 * ((size_t)(kAwTX + 2 * r) + (size_t)(kAwTX + kAwDC - 1 + 2 * r));
+    };
+    if (half && p.disp_range % 8 != 0) {
         go(k_aw_wta<__half, false>, (const __half *)vol);
+    } else if (half) {
+        const size_t psmem = pipe_smem((size_t)kAwHPitch * 2);
+        cudaFuncSetAttribute(k_aw_wta_pipe<__half, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)psmem);
+        k_aw_wta_pipe<__half, false><<<grid, kAwThreads, psmem, c->stream>>>((const __half *)vol, plr, plt, pw, g, raw,
+                                                                             rl, cost_out, H, W, p.disp_range, e);
     } else {
-        const size_t psmem = sizeof(float) * (2 * (size_t)(kAwTX + 2 * r + 4) * kAwCPitch + 2 * (size_t)e * kAwTX +
-                                              2 * (size_t)e * (kAwTX + kAwDC)) +
-                             sizeof(uint32_t) * 3 * ((size_t)(kAwTX + 2 * r) + (size_t)(kAwTX + kAwDC - 1 + 2 * r));
-        cudaFuncSetAttribute(k_aw_wta_pipe<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)psmem);
-        k_aw_wta_pipe<0><<<grid, kAwThreads, psmem, c->stream>>>((const float *)vol, plr, plt, pw, g, raw, rl, cost_out,
-                                                                 H, W, p.disp_range, e);
+        const size_t psmem = pipe_smem((size_t)kAwCPitch * 4);
+        cudaFuncSetAttribute(k_aw_wta_pipe<float, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)psmem);
+        k_aw_wta_pipe<float, true><<<grid, kAwThreads, psmem, c->stream>>>((const float *)vol, plr, plt, pw, g, raw,
+                                                                           rl, cost_out, H, W, p.disp_range, e);
     }
     count_launch(c);
     return check_launch(c, "aw_wta");
