@@ -650,7 +650,7 @@ def run_ours(args, rank, world):
 NCU_BYTES_PER_ENTRY = {("cross_vert_wta", 0): 4.16, ("cross_hseg", 0): 4.00}
 # ncu DRAM bytes of one plain-form adaptive-weight launch (k_aw_wta_pipe, one view)
 # at 640x480, D=64 (profiles/k_aw_wta_pipe_*.md)
-NCU_AW_BYTES = {(640, 480, 64): 85.52e6}
+NCU_AW_BYTES = {(640, 480, 64): 85.61e6}
 
 
 def roofline(stages, name, W, H, D, ag, peaks, src, p, ms_pair=None):
