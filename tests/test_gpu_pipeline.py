@@ -144,6 +144,19 @@ def test_fused_log_census_volume_equals_modules(ctx, W, H, D):
     assert bits_equal(got[3], agg)
 
 
+@pytest.mark.parametrize("W,H,D", [(1, 1, 1), (5, 1, 3), (1, 7, 1), (2, 2, 2), (3, 5, 3)])
+@pytest.mark.parametrize("aggr", [0, 1, 2, 3])
+def test_degenerate_shapes(ctx, oracle_mod, W, H, D, aggr):
+    """Single rows, single columns, D = W, windows reduced to the image: the
+    pipeline (fused or composed, as it chooses) equals the oracle."""
+    rng = np.random.default_rng(W * 100 + H * 10 + D + aggr)
+    L = rng.integers(0, 256, (H, W), dtype=np.uint8)
+    Rr = rng.integers(0, 256, (H, W), dtype=np.uint8)
+    g, o = run_both(ctx, oracle_mod, L, Rr, disp_range=D, cost1=1, cost2=0, aggr=aggr, box_rad=0, aw_rad=0,
+                    cross_arm=3)
+    assert_same(g, o)
+
+
 @pytest.mark.parametrize("c1,c2", [(4, 3), (4, 0), (2, 0)])
 def test_volume_views_equal_composed_modules(ctx, c1, c2):
     """Cross-based views over a precomputed volume (LoG, rank alone) give the
