@@ -1,7 +1,8 @@
 // k_batch.cu -- the cross-based pipeline over a table of views, one launch per
 // stage for a whole batch (one pair = its left and right view).
 //
-// Stages (each a persistent kernel looping over the work items of all views):
+// Stages (each kernel loops over the work items of all views: one block per
+// item by default, or resident blocks striding over them):
 //   prep   block per (image, 64x16 tile): per-pixel records of every image
 //          (census code, colour, horizontal arms) and arm words (horizontal and
 //          vertical arms), in image coordinates, made once per image and read by

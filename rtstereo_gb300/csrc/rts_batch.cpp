@@ -2,12 +2,13 @@
 // (rts_server_*) of the cross-based pipeline.
 //
 // Batched form: the n pairs become 2n views of one view table; every stage is
-// one persistent launch over all views (k_batch.cu).  The five launches (and
-// the reset of the row summaries) are captured once per batch shape into a
-// CUDA graph; a later call with the same shape re-uploads only the view table
-// (its image and output pointers) and replays the graph.  The tile parameters
-// of the stages (rows per vertical block, persistent blocks per SM) are picked
-// per batch shape by timing the candidates on the first call (autotuner).
+// one launch over all views (k_batch.cu).  The five launches (and the reset of
+// the row summaries) are captured once per batch shape into a CUDA graph; a
+// later call with the same shape re-uploads only the view table (its image and
+// output pointers) and replays the graph.  The tile parameters of the stages
+// (rows per vertical block; one block per item, or resident blocks striding
+// over the items and how many per SM) are picked per batch shape by timing the
+// candidates on the first call (autotuner).
 //
 // Serving loop: requests are admitted in arrival order while a slot and enough
 // of the server's device pool (cost-volume bytes of the request, e.g. a 40 GB
@@ -15,11 +16,12 @@
 // streams, so a batch formed from requests that arrived while others were
 // running overlaps with them on the device.  Completion is polled with events.
 // With priority_pixels, requests of at least that many pixels form a second
-// class: each runs alone on a stream of the greatest priority, while the other
-// class's batches run one block per work item, so the large request's blocks
-// are dispatched as soon as the small ones' retire.  Pinned host staging is
-// kept in a cache across requests (pinning pages is slow, and freeing them
-// waits for the device).
+// class: each runs alone on a stream above the small requests' priority (the
+// older large request above the newer), no small request starts while a large
+// one runs, and the small requests' launches have short items, so a large
+// request's blocks are dispatched as soon as the small ones' retire.  Pinned
+// host staging is kept in a cache across requests (pinning pages is slow, and
+// freeing them waits for the device).
 #include <string.h>
 
 #include <algorithm>
@@ -148,8 +150,8 @@ void view_dims(int n, const rts_pair *pairs, const rts_params *params, int right
 }
 
 // Candidate tiles of the autotuner.
-// (strip rows of the vertical kernel, row-segment blocks per SM)
-const CrossTune kTuneCandidates[] = {{4096, 8}, {256, 8}, {96, 8}, {4096, 6}};
+// (strip rows of the vertical kernel, row-segment blocks per SM, persistent)
+const CrossTune kTuneCandidates[] = {{4096, 8, 0}, {256, 8, 0}, {96, 8, 0}, {4096, 8, 1}, {256, 8, 1}, {4096, 6, 1}};
 
 }  // namespace
 
@@ -239,15 +241,19 @@ rts_status rts::batch_views_run(rts_ctx *c, int n, const rts_pair *pairs, const 
         for (const CrossTune &cand : kTuneCandidates) {
             ViewTable t;
             RTS_TRY(upload_views(c, b, cand, nullptr, &t));
-            RTS_CU(c, cudaEventRecord(e0, c->stream));
-            RTS_TRY(launch_cross_views(c, p, t, segk, 0, gray, b.max_d, cand, b.row_last_all, b.row_last_count));
-            RTS_CU(c, cudaEventRecord(e1, c->stream));
-            RTS_CU(c, cudaEventSynchronize(e1));
-            float ms = 0;
-            RTS_CU(c, cudaEventElapsedTime(&ms, e0, e1));
-            if (ms < best_ms) {
-                best_ms = ms;
-                best = cand;
+            // one untimed run (first launches of a kernel carry set-up costs), then
+            // the faster of two timed runs
+            for (int rep = 0; rep < 3; rep++) {
+                RTS_CU(c, cudaEventRecord(e0, c->stream));
+                RTS_TRY(launch_cross_views(c, p, t, segk, 0, gray, b.max_d, cand, b.row_last_all, b.row_last_count));
+                RTS_CU(c, cudaEventRecord(e1, c->stream));
+                RTS_CU(c, cudaEventSynchronize(e1));
+                float ms = 0;
+                RTS_CU(c, cudaEventElapsedTime(&ms, e0, e1));
+                if (rep > 0 && ms < best_ms) {
+                    best_ms = ms;
+                    best = cand;
+                }
             }
         }
         cudaEventDestroy(e0);
@@ -426,6 +432,7 @@ struct Batch {
     cudaEvent_t done = nullptr;
     bool active = false;
     bool high = false;  // on a high-priority stream (large requests, launched alone)
+    int prio = 0;       // the stream's priority (lower numbers are served first)
 };
 
 }  // namespace
@@ -492,13 +499,45 @@ bool is_large(const rts_server *s, const Request &r) {
     return s->cfg.priority_pixels > 0 && (long long)r.pair.width * r.pair.height >= s->cfg.priority_pixels;
 }
 
-// A free stream of the given class, round robin; -1 if none.
+// requests the admission looks past while small ones are held
+constexpr size_t kLookahead = 256;
+
+bool large_running(const rts_server *s) {
+    for (const Batch &b : s->batches)
+        if (b.high && b.active) return true;
+    return false;
+}
+
+// A free stream of the given class; -1 if none.  Small requests take the ring
+// round robin.  The large class's streams form a ladder of priorities: a new
+// large request takes the greatest free priority below that of every large
+// request still running, so the oldest one keeps the SMs it needs and finishes
+// in its own time, rather than every concurrent one being slowed alike (FIFO
+// within the class instead of processor sharing).
 int free_slot(const rts_server *s, bool high) {
-    for (int k = 0; k < (int)s->batches.size(); k++) {
-        const int j = (s->next_stream + k) % (int)s->batches.size();
-        if (!s->batches[j].active && s->batches[j].high == high) return j;
+    const int nb = (int)s->batches.size();
+    if (!high) {
+        for (int k = 0; k < nb; k++) {
+            const int j = (s->next_stream + k) % nb;
+            if (!s->batches[j].active && !s->batches[j].high) return j;
+        }
+        return -1;
     }
-    return -1;
+    bool any = false;
+    int floor_prio = 0;  // the lowest priority (largest number) of the running large requests
+    for (const Batch &b : s->batches)
+        if (b.high && b.active) {
+            floor_prio = any ? std::max(floor_prio, b.prio) : b.prio;
+            any = true;
+        }
+    int below = -1, lowest = -1;
+    for (int j = 0; j < nb; j++) {
+        const Batch &b = s->batches[j];
+        if (!b.high || b.active) continue;
+        if ((!any || b.prio > floor_prio) && (below < 0 || b.prio < s->batches[below].prio)) below = j;
+        if (lowest < 0 || b.prio > s->batches[lowest].prio) lowest = j;
+    }
+    return below >= 0 ? below : lowest;
 }
 
 // Launches the requests in `ids` as one batch on a free stream of their class.
@@ -560,12 +599,10 @@ rts_status launch_batch(rts_server *s, std::vector<Request *> &ids) {
         fill_views(b, n, pairs.data(), outs.data(), right, p.median_ksize ? &med : nullptr);
         ViewTable t;
         CrossTune tune;
-        if (s->cfg.priority_pixels > 0 && !bt.high) {
-            // one block per work item, short items: the blocks of a large request
-            // launched meanwhile on a high-priority stream take the SMs as these retire
-            tune.persistent = 0;
-            tune.vert_rows = 256;
-        }
+        // one block per work item (the default): the blocks of a large request take
+        // the SMs as the small requests' retire, and a block that starts late owns
+        // no share of the items fixed at launch; the small requests' items are short
+        if (s->cfg.priority_pixels > 0 && !bt.high) tune.vert_rows = 256;
         st = upload_views(c, b, tune, nullptr, &t);
         if (st == RTS_OK) st = launch_cross_views(c, p, t, segk, 0, gray, b.max_d, tune, b.row_last_all, b.row_last_count);
     }
@@ -615,19 +652,29 @@ rts_status progress_locked(rts_server *s) {
         else if (q != cudaErrorNotReady) return cuda_check(s->ctx, q, "server batch");
     }
     // admission in arrival order while a stream of the request's class, a slot and
-    // device memory are free; a large request (priority_pixels) goes alone
+    // device memory are free; a large request (priority_pixels) goes alone.  While
+    // a large request runs, the small ones wait (their blocks would share the SMs
+    // with it) and a large one behind them may go first.
     for (;;) {
         while (!s->queue.empty() && s->reqs[s->queue.front()]->state == RQ_CANCELLED) s->queue.pop_front();
         if (s->queue.empty()) return RTS_OK;
-        const bool high = is_large(s, *s->reqs[s->queue.front()]);
+        size_t pos = 0;
+        if (large_running(s)) {
+            const size_t look = std::min(s->queue.size(), kLookahead);
+            while (pos < look && (s->reqs[s->queue[pos]]->state == RQ_CANCELLED ||
+                                  !is_large(s, *s->reqs[s->queue[pos]])))
+                pos++;
+            if (pos == look) return RTS_OK;
+        }
+        const bool high = is_large(s, *s->reqs[s->queue[pos]]);
         if (free_slot(s, high) < 0) return RTS_OK;
         const int max_batch = high ? 1 : s->cfg.max_batch;
         std::vector<Request *> batch;
         size_t batch_bytes = 0;
-        while (!s->queue.empty() && (int)batch.size() < max_batch && s->inflight < s->cfg.max_inflight) {
-            Request &r = *s->reqs[s->queue.front()];
+        while (pos < s->queue.size() && (int)batch.size() < max_batch && s->inflight < s->cfg.max_inflight) {
+            Request &r = *s->reqs[s->queue[pos]];
             if (r.state == RQ_CANCELLED) {
-                s->queue.pop_front();
+                s->queue.erase(s->queue.begin() + pos);
                 continue;
             }
             if (is_large(s, r) != high) break;  // the next request is of the other class
@@ -642,19 +689,19 @@ rts_status progress_locked(rts_server *s) {
             r.d_mem = s->pool.alloc(need);
             if (!r.d_mem) break;
             batch_bytes += need_scratch;
-            s->queue.pop_front();
+            s->queue.erase(s->queue.begin() + pos);
             s->inflight++;
             batch.push_back(&r);
         }
         if (batch.empty()) return RTS_OK;
         rts_status st = launch_batch(s, batch);
         if (st != RTS_OK) {
-            // put the requests back at the head of the queue
+            // put the requests back where they were in the queue
             for (auto it = batch.rbegin(); it != batch.rend(); ++it) {
                 s->pool.release((*it)->d_mem, (*it)->d_bytes);
                 (*it)->d_mem = nullptr;
                 s->inflight--;
-                s->queue.push_front((*it)->ticket);
+                s->queue.insert(s->queue.begin() + pos, (*it)->ticket);
             }
             return st == RTS_ERR_BUSY ? RTS_OK : st;
         }
@@ -677,20 +724,25 @@ rts_status rts_server_create(rts_server **out, rts_ctx *ctx, const rts_server_co
         delete s;
         return set_error(ctx, RTS_ERR_OOM, "cannot reserve the server's device pool");
     }
-    // three streams at the default priority; with priority_pixels, two more at the
-    // greatest priority for the large requests (their blocks are dispatched first)
-    const int nlow = 3, nhigh = cfg->priority_pixels > 0 ? 2 : 0;
+    // three streams at the least priority; with priority_pixels, up to four more
+    // for the large requests at the priorities above it, greatest first (their
+    // blocks are dispatched before the small requests', the older large
+    // request's before the newer's; with a single level above the least, two
+    // streams share it)
     int least = 0, greatest = 0;
     if (cudaDeviceGetStreamPriorityRange(&least, &greatest) != cudaSuccess) {
         delete s;
         return RTS_ERR_CUDA;
     }
+    const int levels = least - greatest;  // priorities above the least
+    const int nlow = 3, nhigh = cfg->priority_pixels > 0 ? (levels >= 2 ? std::min(levels, 4) : 2) : 0;
     s->streams.resize(nlow + nhigh);
     s->batches.resize(nlow + nhigh);
     for (int i = 0; i < nlow + nhigh; i++) {
-        s->batches[i].high = i >= nlow;
-        if (cudaStreamCreateWithPriority(&s->streams[i], cudaStreamNonBlocking, i >= nlow ? greatest : least) !=
-                cudaSuccess ||
+        Batch &b = s->batches[i];
+        b.high = i >= nlow;
+        b.prio = !b.high ? least : levels >= 2 ? greatest + (i - nlow) : greatest;
+        if (cudaStreamCreateWithPriority(&s->streams[i], cudaStreamNonBlocking, b.prio) != cudaSuccess ||
             cudaEventCreateWithFlags(&s->batches[i].done, cudaEventDisableTiming) != cudaSuccess) {
             rts_server_destroy(s);
             return RTS_ERR_CUDA;

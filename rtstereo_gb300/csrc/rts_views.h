@@ -50,7 +50,8 @@ struct ViewTable {
 struct CrossTune {
     int vert_rows = 4096;   // output rows per vertical-aggregation item (a strip of one column)
     int grid_mult = 8;      // persistent blocks per SM of the row-segment kernel
-    int persistent = 1;     // 0: one block per work item (no cap at the resident blocks)
+    int persistent = 0;     // 0: one block per work item (the hardware balances the
+                            // blocks); 1: resident blocks striding over the items
 };
 
 // Per-view item counts (host): the layout the kernels and the planner share.
