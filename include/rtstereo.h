@@ -242,7 +242,8 @@ typedef struct rts_server_config {
     int max_batch;       /* pairs launched together */
     int precision;       /* RTS_PREC_F32 or RTS_PREC_F16 */
     long long priority_pixels; /* 0: one class; else requests of at least this many pixels
-                                  run alone on high-priority streams, the others in batches */
+                                  run alone on high-priority streams (older first), the others
+                                  in batches that do not start while such a request runs */
 } rts_server_config;
 
 typedef struct rts_request_stats {
