@@ -243,7 +243,8 @@ typedef struct rts_server_config {
     int precision;       /* RTS_PREC_F32 or RTS_PREC_F16 */
     long long priority_pixels; /* 0: one class; else requests of at least this many pixels
                                   run alone on high-priority streams (older first), the others
-                                  in batches that do not start while such a request runs */
+                                  in batches that do not start while such a request runs
+                                  (unless the oldest has waited 8 ms) */
 } rts_server_config;
 
 typedef struct rts_request_stats {

@@ -18,10 +18,10 @@
 // With priority_pixels, requests of at least that many pixels form a second
 // class: each runs alone on a stream above the small requests' priority (the
 // older large request above the newer), no small request starts while a large
-// one runs, and the small requests' launches have short items, so a large
-// request's blocks are dispatched as soon as the small ones' retire.  Pinned
-// host staging is kept in a cache across requests (pinning pages is slow, and
-// freeing them waits for the device).
+// one runs (unless it has waited 8 ms), and the small requests' launches have
+// short items, so a large request's blocks are dispatched as soon as the small
+// ones' retire.  Pinned host staging is kept in a cache across requests
+// (pinning pages is slow, and freeing them waits for the device).
 #include <string.h>
 
 #include <algorithm>
@@ -501,6 +501,9 @@ bool is_large(const rts_server *s, const Request &r) {
 
 // requests the admission looks past while small ones are held
 constexpr size_t kLookahead = 256;
+// a small request that has waited this long starts even while a large one runs
+// (no starvation under a steady stream of large requests)
+constexpr double kHoldMs = 8.0;
 
 bool large_running(const rts_server *s) {
     for (const Batch &b : s->batches)
@@ -654,12 +657,13 @@ rts_status progress_locked(rts_server *s) {
     // admission in arrival order while a stream of the request's class, a slot and
     // device memory are free; a large request (priority_pixels) goes alone.  While
     // a large request runs, the small ones wait (their blocks would share the SMs
-    // with it) and a large one behind them may go first.
+    // with it), up to kHoldMs for the oldest, and a large one behind them may go
+    // first.
     for (;;) {
         while (!s->queue.empty() && s->reqs[s->queue.front()]->state == RQ_CANCELLED) s->queue.pop_front();
         if (s->queue.empty()) return RTS_OK;
         size_t pos = 0;
-        if (large_running(s)) {
+        if (large_running(s) && s->now_ms() - s->reqs[s->queue.front()]->t_submit < kHoldMs) {
             const size_t look = std::min(s->queue.size(), kLookahead);
             while (pos < look && (s->reqs[s->queue[pos]]->state == RQ_CANCELLED ||
                                   !is_large(s, *s->reqs[s->queue[pos]])))

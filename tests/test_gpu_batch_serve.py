@@ -111,3 +111,34 @@ def test_server_admission_and_cancel(ctx):
         assert e.value.status == 7  # RTS_ERR_CANCELLED
     finally:
         srv.close()
+
+
+def test_server_large_pair_overtakes_held_small_one(ctx):
+    """priority_pixels: while a large pair runs, a small one waits, and a large pair
+    submitted after it starts first; every result is still the single-pair run's."""
+    import rtstereo_gb300 as R
+    srv = R.Server(ctx, hbm_budget=4 << 30, max_inflight=8, max_batch=2, precision=R.PREC_F16,
+                   priority_pixels=1920 * 1080)
+    try:
+        big = [R.synth_pair(0xB0 + i, 1920, 1080, 128, 8, 1, 2.0, 4)[:2] for i in range(2)]
+        small = R.synth_pair(0xB5, 320, 240, 32, 4, 0, 2.0, 4)[:2]
+        order = [(big[0], 128), (small, 32), (big[1], 128)]
+
+        def run():
+            tickets = []
+            for (L, Rr), D in order:
+                tickets.append(srv.submit(R.params(disp_range=D, precision=R.PREC_F16), L, Rr))
+                srv.progress()
+            return tickets, [srv.wait(t) for t, _ in tickets]
+
+        run()  # warm: the server's pinned staging for these sizes, the kernels
+        tickets, stats = run()
+        # (submit, start, done) in ms: the first large pair runs for milliseconds, so
+        # the small pair is held and the second large pair is launched before it
+        assert stats[2][1] <= stats[1][1]
+        assert stats[1][1] >= stats[0][0]
+        for ((L, Rr), D), (t, outs) in zip(order, tickets):
+            for g, w in zip(outs, single(ctx, L, Rr, D, R.PREC_F16)):
+                assert bits_equal(g, w)
+    finally:
+        srv.close()
