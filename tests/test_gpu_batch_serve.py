@@ -10,12 +10,14 @@ from conftest import bits_equal
 pytestmark = pytest.mark.gpu
 
 MIX = [(160, 120, 32), (96, 64, 64), (200, 90, 16), (128, 128, 128), (64, 48, 32), (250, 60, 64)]
+# disparity ranges above 128: eight 32-disparity chunks per lane, a partial last one
+WIDE = [(300, 40, 256), (96, 64, 64), (260, 33, 200), (180, 20, 130)]
 
 
-def make_pairs(seed0):
+def make_pairs(seed0, mix=MIX):
     import rtstereo_gb300 as R
     out = []
-    for i, (W, H, D) in enumerate(MIX):
+    for i, (W, H, D) in enumerate(mix):
         L, Rr, _ = R.synth_pair(seed0 + i, W, H, D, 4, 1, 2.0, min(4, D - 1))
         out.append((L, Rr, D))
     return out
@@ -26,15 +28,16 @@ def single(ctx, L, Rr, D, prec):
     return ctx.pipeline(R.params(disp_range=D, precision=prec), L, Rr)[:3]
 
 
+@pytest.mark.parametrize("mix", ["mix", "wide"])
 @pytest.mark.parametrize("prec", [0, 1])
-def test_batch_matches_single_runs(ctx, oracle_mod, prec):
+def test_batch_matches_single_runs(ctx, oracle_mod, prec, mix):
     torch = pytest.importorskip("torch")
     import rtstereo_gb300 as R
     s = torch.cuda.Stream()
     ctx.set_stream(s.cuda_stream)
     try:
         for rnd in range(2):  # the second round replays the captured graph with new data
-            data = make_pairs(1000 * rnd + 7)
+            data = make_pairs(1000 * rnd + 7, MIX if mix == "mix" else WIDE)
             dev, pairs, params, outs, bufs = [], [], [], [], []
             for L, Rr, D in data:
                 H, W = L.shape
@@ -55,7 +58,7 @@ def test_batch_matches_single_runs(ctx, oracle_mod, prec):
     finally:
         ctx.set_stream(None)
     # and the plain single-pair run itself equals the oracle for one of them
-    if prec == 0:
+    if prec == 0 and mix == "mix":
         L, Rr, D = make_pairs(7)[0]
         O = oracle_mod
         rgb = lambda a: np.ascontiguousarray(np.repeat(a[:, :, None], 3, axis=2))

@@ -144,6 +144,17 @@ def test_fused_log_census_volume_equals_modules(ctx, W, H, D):
     assert bits_equal(got[3], agg)
 
 
+@pytest.mark.parametrize("W,H,D", [(300, 40, 256), (260, 33, 200), (180, 20, 130)])
+@pytest.mark.parametrize("c1,c2", [(1, 3), (3, 0)])
+def test_cross_wide_disparity_ranges(ctx, oracle_mod, W, H, D, c1, c2):
+    """Disparity ranges above 128 on the cross-based views: eight 32-disparity
+    chunks per lane in the vertical kernel, a partial last chunk; AD + census on
+    float segments, census alone on integer segments."""
+    L, Rr = synth(W + H + D, W, H, D, 3)
+    g, o = run_both(ctx, oracle_mod, L, Rr, disp_range=D, cost1=c1, cost2=c2, aggr=3)
+    assert_same(g, o)
+
+
 @pytest.mark.parametrize("W,H,D", [(1, 1, 1), (5, 1, 3), (1, 7, 1), (2, 2, 2), (3, 5, 3)])
 @pytest.mark.parametrize("aggr", [0, 1, 2, 3])
 def test_degenerate_shapes(ctx, oracle_mod, W, H, D, aggr):
