@@ -40,6 +40,7 @@ WORKLOADS = {
     "cross_384x288_d16": (384, 288, 16, 1, 3, 3, 6, 0, 2.0, 0xC0, {}),
     "cross_1920x1080_d128": (1920, 1080, 128, 1, 3, 3, 24, 2, 3.0, 0xC2, {}),
     "cross_1280x720_d128": (1280, 720, 128, 1, 3, 3, 24, 2, 3.0, 0xC2, {}),
+    "census_cross_1280x720_d128": (1280, 720, 128, 3, 0, 3, 24, 2, 3.0, 0xC2, {}),
     "aw_1920x1080_d128": (1920, 1080, 128, 1, 3, 2, 24, 2, 3.0, 0xC2, {}),
     "rank_census_cross_1920x1080_d128": (1920, 1080, 128, 2, 3, 3, 24, 2, 3.0, 0xC2, {"rank_rad": 3}),
     "box_1920x1080_d128": (1920, 1080, 128, 1, 3, 1, 24, 2, 3.0, 0xC2, {"box_rad": 4}),
@@ -645,9 +646,12 @@ def run_ours(args, rank, world):
 
 
 # DRAM bytes per cost entry of the two cross-based kernels, from one ncu capture
-# of each at 1280x720, D=128 (both views; profiles/cross_views_*.md); a launch at
-# another size moves these per entry
-NCU_BYTES_PER_ENTRY = {("cross_vert_wta", 0): 4.16, ("cross_hseg", 0): 4.00}
+# of each at 1280x720, D=128 (both views; profiles/cross_views_*.md), by form:
+# 0 plain (f32 segments), 1 FP16 (f16 segments), 2 integer costs (u16 segments);
+# a launch at another size moves these per entry
+NCU_BYTES_PER_ENTRY = {("cross_vert_wta", 0): 4.16, ("cross_hseg", 0): 4.00,
+                       ("cross_vert_wta", 1): 2.13, ("cross_hseg", 1): 2.00,
+                       ("cross_vert_wta", 2): 2.13, ("cross_hseg", 2): 2.00}
 # ncu DRAM bytes of one plain-form adaptive-weight launch (k_aw_wta_pipe, one view)
 # at 640x480, D=64 (profiles/k_aw_wta_pipe_*.md)
 NCU_AW_BYTES = {(640, 480, 64): 85.61e6}
@@ -687,7 +691,7 @@ def roofline(stages, name, W, H, D, ag, peaks, src, p, ms_pair=None):
     byts = views * 2 * S * E
     achieved = byts / (per_launch_ms / 1e3) / 1e9
     peak = peaks["hbm_gbs"]
-    bpe = None if int_costs else NCU_BYTES_PER_ENTRY.get((kname, 1 if p.precision else 0))
+    bpe = NCU_BYTES_PER_ENTRY.get((kname, 2 if int_costs else 1 if p.precision else 0))
     out = {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
            "frac": achieved / peak, "traffic": bpe * views * E if bpe else None, "launches": launches,
            "ms_per_launch": per_launch_ms, "bytes_per_launch": byts, "peak_source": src}
