@@ -47,7 +47,7 @@ def test_roofline_fields():
     assert r["kernel"] == "cross_vert_wta" and r["bytes_per_launch"] == 2 * 2 * 4 * E
     assert r["traffic"] == pytest.approx(4.16 * 2 * E)
     assert r["pipeline"]["bytes_per_pair"] == 2 * (4 * 4 * E) + 2 * (8 * 1920 * 1080) + 3 * 1920 * 1080
-    # integer costs keep 2-byte segments (no ncu traffic figure for them)
+    # integer costs keep 2-byte segments, with their own ncu traffic figure
     p = R.params(disp_range=128, cost1=3, cost2=0)
     r = bench.roofline(stages, "census_cross_1920x1080_d128", 1920, 1080, 128, 3, peaks, "measured", p)
-    assert r["bytes_per_launch"] == 2 * 2 * 2 * E and r["traffic"] is None
+    assert r["bytes_per_launch"] == 2 * 2 * 2 * E and r["traffic"] == pytest.approx(2.13 * 2 * E)
