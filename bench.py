@@ -646,14 +646,14 @@ def run_ours(args, rank, world):
 
 
 # DRAM bytes per cost entry of the two cross-based kernels, from one ncu capture
-# of each at 1280x720, D=128 (both views; profiles/cross_views_*.md), by form:
+# of each at 1280x720, D=128 (one launch covers both views), by form:
 # 0 plain (f32 segments), 1 FP16 (f16 segments), 2 integer costs (u16 segments);
 # a launch at another size moves these per entry
 NCU_BYTES_PER_ENTRY = {("cross_vert_wta", 0): 4.16, ("cross_hseg", 0): 4.00,
                        ("cross_vert_wta", 1): 2.13, ("cross_hseg", 1): 2.00,
                        ("cross_vert_wta", 2): 2.13, ("cross_hseg", 2): 2.00}
 # ncu DRAM bytes of one plain-form adaptive-weight launch (k_aw_wta_pipe, one view)
-# at 640x480, D=64 (profiles/k_aw_wta_pipe_*.md)
+# at 640x480, D=64 (the full capture of that launch)
 NCU_AW_BYTES = {(640, 480, 64): 85.61e6}
 
 
