@@ -48,6 +48,10 @@ WORKLOADS = {
     "census_cross_1920x1080_d128": (1920, 1080, 128, 3, 0, 3, 24, 2, 3.0, 0xC2, {}),
     "ncc_box_1920x1080_d128": (1920, 1080, 128, 5, 0, 1, 24, 2, 3.0, 0xC2, {"box_rad": 4, "ncc_hrad": 3,
                                                                             "ncc_wrad": 3}),
+    # smaller cases of the same pipelines (profiling)
+    "ncc_box_1280x720_d128": (1280, 720, 128, 5, 0, 1, 24, 2, 3.0, 0xC2, {"box_rad": 4, "ncc_hrad": 3,
+                                                                          "ncc_wrad": 3}),
+    "log_census_cross_1280x720_d128": (1280, 720, 128, 4, 3, 3, 24, 2, 3.0, 0xC2, {}),
 }
 DEFAULT = "aw_640x480_d64"
 
