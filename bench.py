@@ -246,7 +246,10 @@ def cpu_sample(name, rows, threads):
     (independent processes); returns (MDE/s, seconds, sample description)."""
     import multiprocessing as mp
     (W, H, D, c1, c2, ag, extra), imgs = make_inputs(name)
-    rows = min(rows, H)
+    # a strip keeps every window inside one wrap of its rows (the reference's
+    # adaptive-weight loops wrap once, seq/AdaptiveWeightAggregation.cpp:91-93)
+    rad = extra.get("aw_rad", 16) if ag == 2 else 0
+    rows = min(max(rows, rad + 1), H)
     strips = []
     for t in range(threads):
         y0 = (t * rows) % max(1, H - rows + 1)
@@ -261,14 +264,16 @@ def cpu_sample(name, rows, threads):
 
 
 def _cpu_worker(name, strip):
+    """One strip through the reference's own seq/ functions in its driver's order
+    where that build exists (oracle/_ref), else through the oracle's restatement."""
     import oracle
     W, H, D, c1, c2, ag, rects, planes, sigma, seed, extra = WORKLOADS[name]
     L, Rr, Lc, Rc, Ll, Rl = strip
-    kw = dict(extra)
-    if "rank_rad" in kw:
-        kw["rank_rad"] = kw.pop("rank_rad")
-    p = oracle.params(cost1=c1, cost2=c2, aggr=ag, D=D, **kw)
-    oracle.pipeline(p, L, Rr, Lc, Rc, Ll, Rl)
+    p = oracle.params(cost1=c1, cost2=c2, aggr=ag, D=D, box_inplace=1, **extra)
+    if oracle.have_reference():
+        oracle.ref_pipeline(p, L, Rr, Lc, Rc, Ll, Rl)
+    else:
+        oracle.pipeline(p, L, Rr, Lc, Rc, Ll, Rl)
 
 
 def run_reference(args, rank, world):

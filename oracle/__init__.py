@@ -391,3 +391,87 @@ def pipeline(p: OrcParams, lgray, rgray, lrgb, rrgb, llab=None, rlab=None, want_
     if rc != 0:
         raise RuntimeError("oracle pipeline failed (bad parameters or out of memory)")
     return dl, dr, mk, cost
+
+
+def ref_pipeline(p: OrcParams, lgray, rgray, lrgb, rrgb, llab=None, rlab=None):
+    """The whole pair through the reference's own seq/ functions (oracle/_ref) in
+    its driver's order (seq/Main.cpp:180-257): the left view, the right view as the
+    left-to-right pipeline on the mirrored pair, then cross_check
+    (seq/CrossCheck.cpp:10-23).  The reference's findCross has its own constants
+    (arm 17, threshold 20) and its boxAggregate works in place.  Returns
+    (disp_left, disp_right, mask).  Used as the timed CPU baseline where the
+    reference build exists."""
+    R = reflib()
+    if R is None:
+        raise RuntimeError("the reference's seq/ build (oracle/_ref) is not present")
+    D = p.D
+
+    def view(rg, tg, rc, tc, rl, tl):
+        H, W = rg.shape
+
+        def cost(which, trunc):
+            o = np.zeros((H, W, D), np.float32)
+            if which == 1:  # seq/Main.cpp:183-186
+                if trunc:
+                    R.ref_pixelBasedCostL2R_Color_trunc(ptr(rc), ptr(tc), ptr(o), D, H, W, p.ad_trunc, 0)
+                else:
+                    R.ref_pixelBasedCostL2R_Color(ptr(rc), ptr(tc), ptr(o), D, H, W, 0)
+            elif which == 2:
+                a, b = np.zeros((H, W), np.uint8), np.zeros((H, W), np.uint8)
+                R.ref_calculateRankFilt(ptr(rg), ptr(a), p.rank_rad, H, W)
+                R.ref_calculateRankFilt(ptr(tg), ptr(b), p.rank_rad, H, W)
+                R.ref_pixelBasedL2R(ptr(a), ptr(b), ptr(o), D, H, W)
+            elif which == 3:
+                nb = (2 * p.census_hrad + 1) * (2 * p.census_wrad + 1)
+                a, b = np.zeros((H, W, nb), np.uint8), np.zeros((H, W, nb), np.uint8)
+                R.ref_calcCensusTrans(ptr(rg), ptr(a), p.census_hrad, p.census_wrad, H, W)
+                R.ref_calcCensusTrans(ptr(tg), ptr(b), p.census_hrad, p.census_wrad, H, W)
+                R.ref_calcHammingDist(ptr(a), ptr(b), ptr(o), p.census_hrad, p.census_wrad, H, W, D)
+            elif which == 4:
+                mask = np.ascontiguousarray(LOG5x5, np.float32)
+                a, b = np.zeros((H, W), np.float32), np.zeros((H, W), np.float32)
+                R.ref_convolveImage(ptr(rg), ptr(a), ptr(mask), H, W, 2, 2)
+                R.ref_convolveImage(ptr(tg), ptr(b), ptr(mask), H, W, 2, 2)
+                R.ref_pixelBasedCostL2R_Float(ptr(a), ptr(b), ptr(o), D, H, W)
+            elif which == 5:  # den == 0 cells stay as allocated (zero)
+                R.ref_calcNCCDispL2R(ptr(rg), ptr(tg), ptr(o), D, H, W, p.ncc_hrad, p.ncc_wrad)
+            return o
+
+        c1 = cost(p.cost1, p.aggr == 3)
+        if p.cost2:
+            R.ref_combineCost(ptr(c1), ptr(cost(p.cost2, False)), p.lambda1, p.lambda2, H, W, D)
+        fin = c1
+        if p.aggr == 1:
+            R.ref_boxAggregate(ptr(c1), H, W, D, p.box_rad)
+        elif p.aggr == 2:
+            r = p.aw_rad
+            pw = np.zeros(((2 * r + 1) ** 2,), np.float32)
+            R.ref_calcProxWeight(ptr(pw), p.aw_gamma_p, r)
+            wr = np.zeros((H, W, pw.size), np.float32)
+            wt = np.zeros((H, W, pw.size), np.float32)
+            R.ref_computeWeights(ptr(wr), ptr(pw), ptr(rl), p.aw_gamma_s, H, W, r)
+            R.ref_computeWeights(ptr(wt), ptr(pw), ptr(tl), p.aw_gamma_s, H, W, r)
+            fin = np.zeros_like(c1)
+            R.ref_calcAWCostL2R(ptr(wr), ptr(wt), ptr(c1), ptr(fin), H, W, D, r)
+        elif p.aggr == 3:
+            arms = [np.zeros((H, W, 2), np.int32) for _ in range(4)]
+            R.ref_findCross(ptr(rc), ptr(arms[0]), ptr(arms[2]), H, W)
+            R.ref_findCross(ptr(tc), ptr(arms[1]), ptr(arms[3]), H, W)
+            R.ref_aggregate_cost_horizontal(ptr(c1), H, W, D)
+            fin = np.zeros_like(c1)
+            R.ref_cross_stereo_aggregation(ptr(c1), ptr(fin), *[ptr(a) for a in arms], H, W, D)
+        win = np.zeros((H, W), np.uint8)
+        if p.cost1 == 5 and p.cost2 == 0:
+            R.ref_WTA_NCC(ptr(fin), ptr(win), H, W, D)
+        else:
+            R.ref_WTA(ptr(fin), ptr(win), H, W, D)
+        return win
+
+    flip = lambda a: None if a is None else np.ascontiguousarray(a[:, ::-1])
+    c = lambda a: None if a is None else np.ascontiguousarray(a)
+    dl = view(c(lgray), c(rgray), c(lrgb), c(rrgb), c(llab), c(rlab))
+    dr = flip(view(flip(rgray), flip(lgray), flip(rrgb), flip(lrgb), flip(rlab), flip(llab)))
+    mk = np.zeros_like(dl)
+    H, W = dl.shape
+    R.ref_cross_check(ptr(dl), ptr(dr), ptr(mk), H, W)
+    return dl, dr, mk

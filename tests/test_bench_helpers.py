@@ -51,3 +51,21 @@ def test_roofline_fields():
     p = R.params(disp_range=128, cost1=3, cost2=0)
     r = bench.roofline(stages, "census_cross_1920x1080_d128", 1920, 1080, 128, 3, peaks, "measured", p)
     assert r["bytes_per_launch"] == 2 * 2 * 2 * E and r["traffic"] == pytest.approx(2.13 * 2 * E)
+
+
+def test_reference_arm_line():
+    """bench.py --impl reference on a small strip: one JSON line with the
+    reference-arm keys; the sample runs the reference's own code where it is
+    built (kind "reference"), else the oracle port."""
+    import json
+    import subprocess
+    out = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--steps", "1", "--warmup", "0",
+                          "--cpu-rows", "4", "--workload", "cross_384x288_d16"], cwd=ROOT, capture_output=True,
+                         text=True, timeout=600)
+    assert out.returncode == 0, out.stderr[-2000:]
+    line = json.loads([l for l in out.stdout.splitlines() if l.startswith("{")][-1])
+    import oracle
+    assert line["impl"] == "reference" and line["value"] > 0 and line["unit"] == "MDE/s"
+    assert line["cpu_baseline"]["kind"] == ("reference" if oracle.have_reference() else "port")
+    assert line["cpu_baseline"]["cores"] >= 1 and line["cpu_baseline"]["value"] == line["value"]
+    assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["d2h_bytes_per_step"] == 0

@@ -126,3 +126,23 @@ def test_adaptive_weight(rad):
     a = cost.copy()
     REF.ref_calcAWCostR2L(P(wl), P(wr), P(a), H, W, D, rad)
     assert bits_equal(oracle.aw_r2l(wl, wr, cost, rad, inplace=True), a)
+
+
+@pytest.mark.parametrize("c1,c2,ag,extra", [
+    (1, 3, 3, {}), (1, 3, 1, {"box_rad": 4}), (1, 3, 2, {"aw_rad": 5}), (2, 3, 3, {"rank_rad": 3}),
+    (4, 3, 3, {}), (5, 0, 1, {"box_rad": 2, "ncc_hrad": 3, "ncc_wrad": 3}), (3, 0, 3, {}), (4, 0, 2, {"aw_rad": 3}),
+])
+def test_whole_pipeline_vs_reference_composition(c1, c2, ag, extra):
+    """The oracle's whole-pair pipeline against the reference's own functions
+    composed in its driver's order (oracle.ref_pipeline, also the timed CPU
+    baseline), colour and Lab images distinct from the gray ones; the box in place
+    as the reference does it."""
+    import rtstereo_gb300 as R
+    H, W, D = 30, 64, 16
+    L, Rr, Lc, Rc = pair(c1 * 100 + c2 * 10 + ag, H, W)
+    Ll, Rl = R.rgb_to_lab(Lc), R.rgb_to_lab(Rc)
+    p = oracle.params(D=D, cost1=c1, cost2=c2, aggr=ag, box_inplace=1, **extra)
+    got = oracle.pipeline(p, L, Rr, Lc, Rc, Ll, Rl)[:3]
+    want = oracle.ref_pipeline(p, L, Rr, Lc, Rc, Ll, Rl)
+    for g, w in zip(got, want):
+        assert bits_equal(g, w)
