@@ -392,6 +392,15 @@ def run_batch(args, rank, world):
     ranks_done(world)
 
 
+def latency_target(by_size, size, target_ms):
+    """p99 of one size class against a latency target (None if the class is absent)."""
+    b = by_size.get(size)
+    if not b:
+        return None
+    return {"size": size, "n": b["n"], "target_ms": target_ms, "p99_ms": b["p99"],
+            "from_arrival_p99_ms": b["from_arrival_p99"], "met": b["p99"] < target_ms}
+
+
 def run_serve(args, rank, world):
     """Poisson request stream through rts_server_* (continuous batching)."""
     import rtstereo_gb300 as R
@@ -503,6 +512,9 @@ def run_serve(args, rank, world):
             "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
                            "max": float(lat.max()), "from_arrival_p99": float(np.percentile(arr_lat, 99)),
                            "by_size": by_size, "p99_max_over_ranks": p99_all},
+            # the latency target of the large size class: p99 under 5 ms per 1920x1080 pair,
+            # submit to result (from_arrival adds the host's delay before the submit)
+            "latency_target": latency_target(by_size, "1920x1080", 5.0),
             "one_at_a_time": {"unit": "pairs/s", "value": n / seq_wall, "p50_ms": float(np.percentile(seq_lat, 50)),
                               "p99_ms": float(np.percentile(seq_lat, 99)),
                               "what": "the same arrivals, rts_pipeline_run per pair (HOST buffers), latency from arrival"},

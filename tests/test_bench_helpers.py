@@ -69,3 +69,15 @@ def test_reference_arm_line():
     assert line["cpu_baseline"]["kind"] == ("reference" if oracle.have_reference() else "port")
     assert line["cpu_baseline"]["cores"] >= 1 and line["cpu_baseline"]["value"] == line["value"]
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["d2h_bytes_per_step"] == 0
+
+
+def test_latency_target_record():
+    import bench
+    by = {"1920x1080": {"n": 12, "p99": 4.9, "from_arrival_p99": 5.2}, "320x240": {"n": 3, "p99": 1.0,
+                                                                             "from_arrival_p99": 1.1}}
+    r = bench.latency_target(by, "1920x1080", 5.0)
+    assert r == {"size": "1920x1080", "n": 12, "target_ms": 5.0, "p99_ms": 4.9, "from_arrival_p99_ms": 5.2,
+                 "met": True}
+    assert bench.latency_target(by, "1280x720", 5.0) is None
+    by["1920x1080"]["p99"] = 5.0
+    assert bench.latency_target(by, "1920x1080", 5.0)["met"] is False
