@@ -145,3 +145,39 @@ def test_server_large_pair_overtakes_held_small_one(ctx):
                 assert bits_equal(g, w)
     finally:
         srv.close()
+
+
+def test_server_cancel_while_held(ctx):
+    """A small request cancelled while held behind a running large one leaves the
+    queue cleanly; the large requests around it finish with their single-pair
+    results."""
+    import rtstereo_gb300 as R
+    srv = R.Server(ctx, hbm_budget=4 << 30, max_inflight=8, max_batch=2, precision=R.PREC_F16,
+                   priority_pixels=1920 * 1080)
+    try:
+        big = [R.synth_pair(0xC0 + i, 1920, 1080, 64, 8, 1, 2.0, 4)[:2] for i in range(2)]
+        small = [R.synth_pair(0xC5 + i, 320, 240, 32, 4, 0, 2.0, 4)[:2] for i in range(2)]
+        p = lambda D: R.params(disp_range=D, precision=R.PREC_F16)
+        # warm: pinned staging for these sizes (pinning pages takes milliseconds,
+        # long enough for the first large pair to finish before the small one arrives)
+        for t, _ in [srv.submit(p(64), *big[0]), srv.submit(p(32), *small[0]), srv.submit(p(32), *small[1]),
+                     srv.submit(p(64), *big[1])]:
+            srv.wait(t)
+        ta, oa = srv.submit(p(64), *big[0])
+        srv.progress()
+        ts1, _ = srv.submit(p(32), *small[0])
+        ts2, os2 = srv.submit(p(32), *small[1])
+        assert srv.cancel(ts1) == 0
+        tb, ob = srv.submit(p(64), *big[1])
+        srv.progress()
+        srv.wait(ta)
+        srv.wait(tb)
+        srv.wait(ts2)
+        with pytest.raises(R.RtsError) as e:
+            srv.wait(ts1)
+        assert e.value.status == 7  # RTS_ERR_CANCELLED
+        for (L, Rr), D, outs in ((big[0], 64, oa), (big[1], 64, ob), (small[1], 32, os2)):
+            for g, w in zip(outs, single(ctx, L, Rr, D, R.PREC_F16)):
+                assert bits_equal(g, w)
+    finally:
+        srv.close()
