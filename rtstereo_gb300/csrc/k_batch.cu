@@ -339,9 +339,14 @@ __global__ void __launch_bounds__(kHsegW * 32, 8) k_hseg_views(ViewTable t, Cost
 constexpr int kVertW = 8;
 constexpr int kVertT = kVertW * 32;
 
-// ring depth in rows for arm length L: ticks before the first step plus one
-// (a tick may be written while slower warps still read the previous step)
-static int vert_depth(int L) { return 8 * ((2 * L + 8 + 7) / 8 + 1); }
+// ring depth in rows for arm length L.  A warp may write the next tick while a
+// slower warp still reads the previous step (one barrier per step): the newest
+// row then written is ra + 8 (T0 + s) - 1, the oldest row still read is
+// y0 + 8 (s - 1) - L, and with T0 = ceil((y0 - ra + 8 + L) / 8) they are at most
+// 2L + 22 rows apart (y0 - ra a multiple of 8, e.g. a strip at the image top).
+// The ring holds 2L + 23 rows or more, so the two never share a slot; a whole
+// number of ticks, even (two-row blocks never straddle the wrap).
+static int vert_depth(int L) { return 8 * ((2 * L + 23 + 7) / 8); }
 
 // The ring accumulators: where a row lies in a disparity's arm, its segment is
 // added to the sum and its pixel count to the count, as predicated instructions
