@@ -12,8 +12,15 @@ W*H*D per pair-step (both views) / time.
                Lab) and D2H of both disparity maps and the mask inside the timed step
   roofline     the dominant kernel (stage timer around its launches, CUDA events)
   cpu_baseline the CPU oracle on a bounded sample of the same workload
+  f16          (default line) the FP16 form of the same pair: MDE/s, ratio to the plain
+               form, disparity agreement, cost error against FP64 on sampled rows
+  c2_cross_1080p (default line) the 1920x1080, D=128 cross-based pipeline, plain and
+               FP16 forms, against the stage model's HBM roofline
+  serve        (default line) a Poisson stream of mixed pairs through the serving loop
+               at --serve-rate pairs/s: per-size p50/p99 and pairs/s
   --impl reference  the CPU implementation (oracle/_ref if built here, else the oracle
-               port) on all host cores, same metric
+               port) on all host cores, same metric and config; its inputs come from the
+               oracle's copy of the generator, so it never loads the library
 
 Multi-GPU (torchrun, N>1): independent pairs per rank (weak scaling, no collective on
 the data path); the time reported is the max over ranks.
@@ -56,13 +63,28 @@ WORKLOADS = {
 DEFAULT = "aw_640x480_d64"
 
 
-def make_inputs(name):
-    import rtstereo_gb300 as R
+def make_inputs(name, gen=None):
+    """The workload's pair and its colour / Lab images.  gen: a module with
+    synth_pair / gray_to_rgb / rgb_to_lab -- the library (default), or the
+    oracle's restatement of the same generator for the CPU reference arm, which
+    must not load the library (the two are bit-identical, tests/test_oracle_synth.py)."""
+    if gen is None:
+        import rtstereo_gb300 as gen
     W, H, D, c1, c2, ag, rects, planes, sigma, seed, extra = WORKLOADS[name]
-    L, Rr, _ = R.synth_pair(seed, W, H, D, rects, planes, sigma, min(4, D - 1))
-    Lc, Rc = R.gray_to_rgb(L), R.gray_to_rgb(Rr)
-    Ll, Rl = R.rgb_to_lab(Lc), R.rgb_to_lab(Rc)
+    L, Rr, _ = gen.synth_pair(seed, W, H, D, rects, planes, sigma, min(4, D - 1))
+    Lc, Rc = gen.gray_to_rgb(L), gen.gray_to_rgb(Rr)
+    Ll, Rl = gen.rgb_to_lab(Lc), gen.rgb_to_lab(Rc)
     return (W, H, D, c1, c2, ag, extra), (L, Rr, Lc, Rc, Ll, Rl)
+
+
+def workload_config(name, precision, world):
+    """The `config` object of a bench line; the GPU arm and the CPU reference arm
+    print the same one for the same workload."""
+    W, H, D, c1, c2, ag = WORKLOADS[name][:6]
+    return {"workload": name, "width": W, "height": H, "disp_range": D,
+            "pipeline": "cost1=%d cost2=%d aggr=%d, both views + cross check" % (c1, c2, ag),
+            "precision": precision, "l2": "flushed (256 MB write) before every timed step",
+            "parallelism": f"replicas{world}"}
 
 
 def f64_aw_rows(L, Rr, Lc, Rc, Ll, Rl, D, rad, gamma_s, gamma_p, lam1, lam2, rows, hr, wr):
@@ -241,26 +263,44 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def cpu_sample(name, rows, threads):
-    """Time the CPU oracle pipeline on `threads` strips of `rows` rows each
-    (independent processes); returns (MDE/s, seconds, sample description)."""
-    import multiprocessing as mp
-    (W, H, D, c1, c2, ag, extra), imgs = make_inputs(name)
-    # a strip keeps every window inside one wrap of its rows (the reference's
-    # adaptive-weight loops wrap once, seq/AdaptiveWeightAggregation.cpp:91-93)
-    rad = extra.get("aw_rad", 16) if ag == 2 else 0
-    rows = min(max(rows, rad + 1), H)
-    strips = []
-    for t in range(threads):
-        y0 = (t * rows) % max(1, H - rows + 1)
-        strips.append(tuple(np.ascontiguousarray(a[y0:y0 + rows]) for a in imgs))
-    ctx = mp.get_context("spawn")
-    t0 = time.perf_counter()
-    with ctx.Pool(threads) as pool:
-        pool.starmap(_cpu_worker, [(name, s) for s in strips])
-    dt = time.perf_counter() - t0
-    mde = threads * W * rows * D / dt / 1e6
-    return mde, dt, f"{threads} x ({W}x{rows} strip, D={D}, full pipeline both views + cross check)"
+class CpuSampler:
+    """Times the CPU pipeline on `threads` strips of `rows` rows each of the
+    workload's pair, one strip per worker process of a pool made once (its start
+    is outside every timed sample).  Workers run the oracle single-threaded."""
+
+    def __init__(self, name, rows, threads, gen=None):
+        import multiprocessing as mp
+        (W, H, D, c1, c2, ag, extra), imgs = make_inputs(name, gen)
+        # a strip keeps every window inside one wrap of its rows (the reference's
+        # adaptive-weight loops wrap once, seq/AdaptiveWeightAggregation.cpp:91-93)
+        rad = extra.get("aw_rad", 16) if ag == 2 else 0
+        rows = min(max(rows, rad + 1), H)
+        self.strips = []
+        for t in range(threads):
+            y0 = (t * rows) % max(1, H - rows + 1)
+            self.strips.append(tuple(np.ascontiguousarray(a[y0:y0 + rows]) for a in imgs))
+        self.name, self.threads = name, threads
+        self.mde = threads * W * rows * D / 1e6
+        self.sample = f"{threads} x ({W}x{rows} strip, D={D}, full pipeline both views + cross check)"
+        os.environ["OMP_NUM_THREADS"] = "1"  # inherited by the spawned workers
+        self.pool = mp.get_context("spawn").Pool(threads)
+        self.pool.starmap(_cpu_warm, [() for _ in range(threads)])
+
+    def run(self):
+        """One timed sample: (MDE/s, seconds)."""
+        t0 = time.perf_counter()
+        self.pool.starmap(_cpu_worker, [(self.name, s) for s in self.strips])
+        dt = time.perf_counter() - t0
+        return self.mde / dt, dt
+
+    def close(self):
+        self.pool.close()
+        self.pool.join()
+
+
+def _cpu_warm():
+    import oracle
+    oracle.lib()
 
 
 def _cpu_worker(name, strip):
@@ -284,20 +324,24 @@ def run_reference(args, rank, world):
     oracle.build()
     kind = "reference" if oracle.have_reference() else "port"
     threads = os.cpu_count() or 1
-    rows = args.cpu_rows
+    # inputs from the oracle's copy of the generator: this arm never loads the library
+    cs = CpuSampler(name, args.cpu_rows, threads, gen=oracle)
     vals = []
-    for i in range(args.warmup + args.steps):
-        mde, dt, sample = cpu_sample(name, rows, threads)
-        if i >= args.warmup:
-            vals.append((mde, dt))
+    try:
+        for i in range(args.warmup + args.steps):
+            mde, dt = cs.run()
+            if i >= args.warmup:
+                vals.append((mde, dt))
+    finally:
+        cs.close()
     mde = float(np.mean([v[0] for v in vals]))
     ms = float(np.mean([v[1] for v in vals]) * 1000)
-    W, H, D = WORKLOADS[name][:3]
     line = {"impl": "reference", "metric": "MDE/s", "value": mde, "unit": "MDE/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic random-dot stereo pair",
-            "config": {"workload": name, "width": W, "height": H, "disp_range": D},
-            "cpu_baseline": {"value": mde, "unit": "MDE/s", "cores": threads, "kind": kind, "sample": sample},
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic random-dot stereo pair (seeded, no dataset)",
+            "config": workload_config(name, args.precision, world),
+            "cpu_baseline": {"value": mde, "unit": "MDE/s", "cores": threads, "kind": kind, "sample": cs.sample},
             "e2e": {"value": mde, "unit": "MDE/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     if kind == "port":
         line["note"] = "the reference's seq/ sources are not present on this host; the C oracle port is timed"
@@ -401,22 +445,21 @@ def latency_target(by_size, size, target_ms):
             "from_arrival_p99_ms": b["from_arrival_p99"], "met": b["p99"] < target_ms}
 
 
-def run_serve(args, rank, world):
-    """Poisson request stream through rts_server_* (continuous batching)."""
-    import rtstereo_gb300 as R
-    dev = int(os.environ.get("LOCAL_RANK", "0"))
+def serve_measure(ctx, rate, requests, budget_gb, max_batch, priority_pixels, precision, world):
+    """A Poisson request stream through rts_server_* (continuous batching), then
+    the same arrivals one pair at a time through rts_pipeline_run; returns the
+    line's fields (latency per size class, pairs/s, clocks)."""
     import torch
-    torch.cuda.set_device(dev)
-    dist_init(world)
-    prec = R.PREC_F16 if args.precision == "f16" else R.PREC_F32
+
+    import rtstereo_gb300 as R
+    prec = R.PREC_F16 if precision == "f16" else R.PREC_F32
     pool = mixed_pairs(32, 0xC4000)
     rng = np.random.default_rng(0xC4)
-    n = args.requests
-    arrivals = np.cumsum(rng.exponential(1.0 / args.rate, n))
+    n = requests
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, n))
     choice = rng.integers(len(pool), size=n)
-    ctx = R.Context(dev)
-    srv = R.Server(ctx, hbm_budget=int(args.budget_gb * (1 << 30)), max_inflight=64, max_batch=args.max_batch,
-                   precision=prec, priority_pixels=args.priority_pixels)
+    srv = R.Server(ctx, hbm_budget=int(budget_gb * (1 << 30)), max_inflight=64, max_batch=max_batch,
+                   precision=prec, priority_pixels=priority_pixels)
     # result buffers: pinned host arrays the device writes directly, reused once a
     # request has been collected
     free_outs = {}
@@ -439,8 +482,6 @@ def run_serve(args, rank, world):
             srv.wait(t)
             free_outs[outs[0].shape].append(outs)
     ranks_barrier(world)
-    t0 = time.perf_counter()
-    i = 0
     mde = 0.0
     delay = np.zeros(n)  # arrival -> accepted by the server (host side)
     lat, queue, run = np.zeros(n), np.zeros(n), np.zeros(n)
@@ -451,21 +492,25 @@ def run_serve(args, rank, world):
         lat[k], queue[k], run[k] = done - sub, start - sub, done - start
         free_outs[outs[0].shape].append(outs)
 
-    while i < n:
-        now = time.perf_counter() - t0
-        while i < n and arrivals[i] <= now:
-            L, Rr, D = pool[choice[i]]
-            t, outs = submit(L, Rr, D)
-            pending.append((t, i, outs))
-            delay[i] = (time.perf_counter() - t0 - arrivals[i]) * 1e3
-            mde += L.shape[0] * L.shape[1] * D / 1e6
-            i += 1
-        srv.progress()
-        while pending and srv.poll(pending[0][0]) == 1:
+    dev = torch.cuda.current_device()
+    with ClockSampler(dev) as clk:
+        t0 = time.perf_counter()
+        i = 0
+        while i < n:
+            now = time.perf_counter() - t0
+            while i < n and arrivals[i] <= now:
+                L, Rr, D = pool[choice[i]]
+                t, outs = submit(L, Rr, D)
+                pending.append((t, i, outs))
+                delay[i] = (time.perf_counter() - t0 - arrivals[i]) * 1e3
+                mde += L.shape[0] * L.shape[1] * D / 1e6
+                i += 1
+            srv.progress()
+            while pending and srv.poll(pending[0][0]) == 1:
+                collect(*pending.popleft())
+        while pending:
             collect(*pending.popleft())
-    while pending:
-        collect(*pending.popleft())
-    wall = time.perf_counter() - t0
+        wall = time.perf_counter() - t0
     srv.close()
     # the same arrivals served one pair at a time by the plain call (rts_pipeline_run,
     # HOST buffers, synchronous): latency from arrival, queueing included
@@ -480,7 +525,6 @@ def run_serve(args, rank, world):
         ctx.pipeline(R.params(disp_range=D, precision=prec), L, Rr)
         seq_lat[k] = (time.perf_counter() - t1 - arrivals[k]) * 1e3
     seq_wall = time.perf_counter() - t1
-    lat, queue, run = np.array(lat), np.array(queue), np.array(run)
     arr_lat = lat + delay  # from the request's arrival (the host's submit delay added)
     # per size class (the 1920x1080 pairs carry the latency target); the parts of
     # a request's latency: waiting for admission, then launch to completion seen
@@ -501,14 +545,11 @@ def run_serve(args, rank, world):
     wall = ranks_max([wall], world)[0]
     served, mde = ranks_sum([n, mde], world)
     p99_all = ranks_max([float(np.percentile(lat, 99))], world)[0]
-    line = {"metric": "pairs/s", "value": served / wall, "unit": "pairs/s", "n_gpus": world, "steps": n, "warmup": 2 * len(pool),
-            "ms_per_step": wall * 1e3 / n, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": args.precision, "data": "synthetic random-dot stereo pairs (seeded)",
-            "config": {"workload": "serve_poisson", "requests": n, "rate_per_s": args.rate,
-                       "hbm_budget_gb": args.budget_gb, "max_batch": args.max_batch,
-                       "priority_pixels": args.priority_pixels, "outputs": "pinned host arrays, reused",
-                       "sizes": MIX_SIZES,
-                       "disp": MIX_DISP},
+    return {"value": served / wall, "unit": "pairs/s", "wall_s": wall, "requests": n, "offered_per_s": rate,
+            "config": {"workload": "serve_poisson", "requests": n, "rate_per_s": rate, "hbm_budget_gb": budget_gb,
+                       "max_batch": max_batch, "priority_pixels": priority_pixels, "precision": precision,
+                       "outputs": "pinned host arrays, reused", "sizes": MIX_SIZES, "disp": MIX_DISP,
+                       "pipeline": "AD+census, cross-based, both views + cross check"},
             "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
                            "max": float(lat.max()), "from_arrival_p99": float(np.percentile(arr_lat, 99)),
                            "by_size": by_size, "p99_max_over_ranks": p99_all},
@@ -518,149 +559,216 @@ def run_serve(args, rank, world):
             "one_at_a_time": {"unit": "pairs/s", "value": n / seq_wall, "p50_ms": float(np.percentile(seq_lat, 50)),
                               "p99_ms": float(np.percentile(seq_lat, 99)),
                               "what": "the same arrivals, rts_pipeline_run per pair (HOST buffers), latency from arrival"},
-            "MDE_per_s": mde / wall}
-    if rank == 0:
-        print(json.dumps(line), flush=True)
-    ranks_done(world)
+            "MDE_per_s": mde / wall, "clocks": clk.summary()}
 
 
-def run_ours(args, rank, world):
+def run_serve(args, rank, world):
+    """Poisson request stream through rts_server_* (continuous batching)."""
     import torch
 
     import rtstereo_gb300 as R
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(dev)
     dist_init(world)
-    name = args.workload
-    (W, H, D, c1, c2, ag, extra), (L, Rr, Lc, Rc, Ll, Rl) = make_inputs(name)
-    prec = R.PREC_F16 if args.precision == "f16" else R.PREC_F32
-    p = R.params(cost1=c1, cost2=c2, aggr=ag, disp_range=D, precision=prec, **extra)
     ctx = R.Context(dev)
-    # a dedicated (non-default) stream: the library launches on it, the events record on it
-    stream = torch.cuda.Stream(device=dev)
-    torch.cuda.set_stream(stream)
-    ctx.set_stream(stream.cuda_stream)
+    r = serve_measure(ctx, args.rate, args.requests, args.budget_gb, args.max_batch, args.priority_pixels,
+                      args.precision, world)
+    line = {"metric": "pairs/s", "value": r["value"], "unit": "pairs/s", "n_gpus": world, "steps": r["requests"],
+            "warmup": 64, "ms_per_step": r["wall_s"] * 1e3 / r["requests"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": args.precision,
+            "data": "synthetic random-dot stereo pairs (seeded)", "config": r["config"],
+            **{k: r[k] for k in ("latency_ms", "latency_target", "one_at_a_time", "MDE_per_s", "clocks")}}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    ranks_done(world)
 
-    # device-resident inputs and outputs; a pipeline gets the images it reads:
-    # the cross-based one gray images only (colour = gray in three channels, as the
-    # reference driver reads a gray file), adaptive weights also RGB and Lab
-    gray_only = ag == 3
-    t = lambda a: torch.from_numpy(a).to(f"cuda:{dev}")
-    dL, dR, dLc, dRc, dLl, dRl = (t(a) for a in (L, Rr, Lc, Rc, Ll, Rl))
-    ptr = lambda a: None if gray_only else a.data_ptr()
-    o_dl = torch.empty((H, W), dtype=torch.uint8, device=f"cuda:{dev}")
-    o_dr = torch.empty_like(o_dl)
-    o_mk = torch.empty_like(o_dl)
-    pair = R.Pair(W, H, dL.data_ptr(), dR.data_ptr(), ptr(dLc), ptr(dRc), ptr(dLl), ptr(dRl))
-    out = R.Out(o_dl.data_ptr(), o_dr.data_ptr(), o_mk.data_ptr(), None)
-    import ctypes as C
-    lib = R.lib()
 
-    def step():
-        ctx.check(lib.rts_pipeline_run(ctx.h, R.DEVICE, C.byref(pair), C.byref(p), C.byref(out)), "pipeline")
+class Bench:
+    """One GPU's context and launching stream, and the measurement of one
+    workload's pipeline step through the public call (rts_pipeline_run)."""
 
-    flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{dev}")
-    for _ in range(args.warmup):
-        step()
-    torch.cuda.synchronize()
+    def __init__(self, dev, world, steps, warmup):
+        import torch
 
-    # timed region: per-step events, L2 flushed before each step (outside the events)
-    launches0 = ctx.kernel_launches
-    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    ranks_barrier(world)
-    torch.cuda.synchronize()
-    with ClockSampler(dev) as clk:
-        t0 = time.perf_counter()
-        for i in range(args.steps):
-            flush.zero_()
-            evs[i][0].record(stream)
+        import rtstereo_gb300 as R
+        self.dev, self.world, self.steps, self.warmup = dev, world, steps, warmup
+        self.ctx = R.Context(dev)
+        # a dedicated (non-default) stream: the library launches on it, the events record on it
+        self.stream = torch.cuda.Stream(device=dev)
+        torch.cuda.set_stream(self.stream)
+        self.ctx.set_stream(self.stream.cuda_stream)
+        self.flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{dev}")
+        self.sms = torch.cuda.get_device_properties(dev).multi_processor_count
+
+    def measure(self, name, precision):
+        import ctypes as C
+
+        import torch
+
+        import rtstereo_gb300 as R
+        dev, world, ctx, stream, flush = self.dev, self.world, self.ctx, self.stream, self.flush
+        (W, H, D, c1, c2, ag, extra), imgs = make_inputs(name)
+        L, Rr, Lc, Rc, Ll, Rl = imgs
+        prec = R.PREC_F16 if precision == "f16" else R.PREC_F32
+        p = R.params(cost1=c1, cost2=c2, aggr=ag, disp_range=D, precision=prec, **extra)
+        # device-resident inputs and outputs; a pipeline gets the images it reads:
+        # the cross-based one gray images only (colour = gray in three channels, as the
+        # reference driver reads a gray file), adaptive weights also RGB and Lab
+        gray_only = ag == 3
+        t = lambda a: torch.from_numpy(a).to(f"cuda:{dev}")
+        dL, dR, dLc, dRc, dLl, dRl = (t(a) for a in imgs)
+        ptr = lambda a: None if gray_only else a.data_ptr()
+        o_dl = torch.empty((H, W), dtype=torch.uint8, device=f"cuda:{dev}")
+        o_dr = torch.empty_like(o_dl)
+        o_mk = torch.empty_like(o_dl)
+        pair = R.Pair(W, H, dL.data_ptr(), dR.data_ptr(), ptr(dLc), ptr(dRc), ptr(dLl), ptr(dRl))
+        out = R.Out(o_dl.data_ptr(), o_dr.data_ptr(), o_mk.data_ptr(), None)
+        lib = R.lib()
+
+        def step():
+            ctx.check(lib.rts_pipeline_run(ctx.h, R.DEVICE, C.byref(pair), C.byref(p), C.byref(out)), "pipeline")
+
+        for _ in range(self.warmup):
             step()
-            evs[i][1].record(stream)
         torch.cuda.synchronize()
-        wall = time.perf_counter() - t0
-    ranks_barrier(world)
-    launches = ctx.kernel_launches - launches0
-    ms_steps = [a.elapsed_time(b) for a, b in evs]
-    ms = float(np.mean(ms_steps))
-    # per-kernel times from the library's stage timer (CUDA events around every
-    # launch on the launching stream), on extra steps outside the timed region
-    ctx.enable_stage_timing(True)
-    ctx.reset_stage_times()
-    for i in range(args.steps):
-        flush.zero_()
-        step()
-    torch.cuda.synchronize()
-    stages = ctx.stage_times()
-    ctx.enable_stage_timing(False)
-    ms = ranks_max([ms], world)[0]
-    mde_pair = W * H * D / 1e6
-    value = world * mde_pair / (ms / 1e3)
-
-    # e2e: HOST (pinned) buffers through the same public call
-    pin = lambda a: torch.from_numpy(a).pin_memory()
-    hL, hR, hLc, hRc, hLl, hRl = (pin(a) for a in (L, Rr, Lc, Rc, Ll, Rl))
-    ho = [torch.empty((H, W), dtype=torch.uint8).pin_memory() for _ in range(3)]
-    hpair = R.Pair(W, H, hL.data_ptr(), hR.data_ptr(), ptr(hLc), ptr(hRc), ptr(hLl), ptr(hRl))
-    hout = R.Out(ho[0].data_ptr(), ho[1].data_ptr(), ho[2].data_ptr(), None)
-
-    def hstep():
-        ctx.check(lib.rts_pipeline_run(ctx.h, R.HOST, C.byref(hpair), C.byref(p), C.byref(hout)), "pipeline")
-
-    for _ in range(max(1, args.warmup)):
-        hstep()
-    e_ms = []
-    for i in range(args.steps):
-        flush.zero_()
+        # timed region: per-step events, L2 flushed before each step (outside the events)
+        launches0 = ctx.kernel_launches
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+               for _ in range(self.steps)]
+        ranks_barrier(world)
         torch.cuda.synchronize()
-        t1 = time.perf_counter()
-        hstep()
-        e_ms.append((time.perf_counter() - t1) * 1e3)
-    e2e_ms = float(np.mean(e_ms))
-    e2e_ms = ranks_max([e2e_ms], world)[0]
-    h2d = sum(a.numel() for a in ((hL, hR) if gray_only else (hL, hR, hLc, hRc, hLl, hRl)))
-    d2h = 3 * W * H
+        with ClockSampler(dev) as clk:
+            t0 = time.perf_counter()
+            for i in range(self.steps):
+                flush.zero_()
+                evs[i][0].record(stream)
+                step()
+                evs[i][1].record(stream)
+            torch.cuda.synchronize()
+            wall = time.perf_counter() - t0
+        ranks_barrier(world)
+        launches = ctx.kernel_launches - launches0
+        ms = float(np.mean([a.elapsed_time(b) for a, b in evs]))
+        # per-kernel times from the library's stage timer (CUDA events around every
+        # launch on the launching stream), on extra steps outside the timed region
+        ctx.enable_stage_timing(True)
+        ctx.reset_stage_times()
+        for i in range(self.steps):
+            flush.zero_()
+            step()
+        torch.cuda.synchronize()
+        stages = ctx.stage_times()
+        ctx.enable_stage_timing(False)
+        ms = ranks_max([ms], world)[0]
+        mde_pair = W * H * D / 1e6
+        # e2e: HOST (pinned) buffers through the same public call
+        pin = lambda a: torch.from_numpy(a).pin_memory()
+        hL, hR, hLc, hRc, hLl, hRl = (pin(a) for a in imgs)
+        ho = [torch.empty((H, W), dtype=torch.uint8).pin_memory() for _ in range(3)]
+        hpair = R.Pair(W, H, hL.data_ptr(), hR.data_ptr(), ptr(hLc), ptr(hRc), ptr(hLl), ptr(hRl))
+        hout = R.Out(ho[0].data_ptr(), ho[1].data_ptr(), ho[2].data_ptr(), None)
 
-    # parity spot check of this run's output against the last device run
-    agree = bool(np.array_equal(ho[0].numpy(), o_dl.cpu().numpy()))
-    # FP16 form: share of disparities (both views) equal to the plain form's
-    f16_agree = None
-    if prec == R.PREC_F16:
-        p32 = R.params(cost1=c1, cost2=c2, aggr=ag, disp_range=D, precision=R.PREC_F32, **extra)
-        ref = [torch.empty((H, W), dtype=torch.uint8).pin_memory() for _ in range(3)]
-        rout = R.Out(ref[0].data_ptr(), ref[1].data_ptr(), ref[2].data_ptr(), None)
-        ctx.check(lib.rts_pipeline_run(ctx.h, R.HOST, C.byref(hpair), C.byref(p32), C.byref(rout)), "pipeline")
-        f16_agree = {"disp_left": float((ref[0].numpy() == ho[0].numpy()).mean()),
-                     "disp_right": float((ref[1].numpy() == ho[1].numpy()).mean()),
-                     "mask": float((ref[2].numpy() == ho[2].numpy()).mean())}
-        if ag == 2 and rank == 0:
-            f16_agree["cost_error_vs_f64"] = aw_cost_error_vs_f64(ctx, R, p, p32, L, Rr, Lc, Rc, Ll, Rl)
+        def hstep():
+            ctx.check(lib.rts_pipeline_run(ctx.h, R.HOST, C.byref(hpair), C.byref(p), C.byref(hout)), "pipeline")
 
+        for _ in range(max(1, self.warmup)):
+            hstep()
+        e_ms = []
+        for i in range(self.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            t1 = time.perf_counter()
+            hstep()
+            e_ms.append((time.perf_counter() - t1) * 1e3)
+        e2e_ms = ranks_max([float(np.mean(e_ms))], world)[0]
+        h2d = sum(a.numel() for a in ((hL, hR) if gray_only else (hL, hR, hLc, hRc, hLl, hRl)))
+        # the HOST run's result is the device run's
+        agree = bool(np.array_equal(ho[0].numpy(), o_dl.cpu().numpy()))
+        peaks, src = measured_peaks()
+        roof = roofline(stages, name, W, H, D, ag, peaks, src, p, ms, self.sms)
+        return {"name": name, "precision": precision, "params": p, "imgs": imgs, "W": W, "H": H, "D": D, "ag": ag,
+                "value": world * mde_pair / (ms / 1e3), "ms": ms, "wall_s": wall, "gpu_launches": launches,
+                "e2e": {"value": world * mde_pair / (e2e_ms / 1e3), "unit": "MDE/s", "ms_per_step": e2e_ms,
+                        "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": 3 * W * H,
+                        "host_equals_device_result": agree},
+                "stages_ms_per_step": {k: v[1] / self.steps for k, v in stages.items()},
+                "roofline": roof, "clocks": clk.summary(), "out": [a.numpy().copy() for a in ho]}
+
+
+def agreement(a, b):
+    """Share of equal disparities (both views) and mask cells of two runs."""
+    return {"disp_left": float((a[0] == b[0]).mean()), "disp_right": float((a[1] == b[1]).mean()),
+            "mask": float((a[2] == b[2]).mean())}
+
+
+def c2_cross_record(bench, peaks):
+    """The 1920x1080, D=128 cross-based pipeline (plain and FP16 forms) against
+    the stage model's HBM roofline."""
+    name = "cross_1920x1080_d128"
+    m = bench.measure(name, "f32")
+    m16 = bench.measure(name, "f16")
+    roof = m["roofline"]
+    bp = roof["pipeline"]["bytes_per_pair"]
+    target_ms = bp / (0.6 * peaks["hbm_gbs"] * 1e9) * 1e3  # 60 % of the measured copy bandwidth
+    return {"workload": name, "ms_per_pair": m["ms"], "value": m["value"], "unit": "MDE/s",
+            "e2e_ms_per_pair": m["e2e"]["ms_per_step"], "pipeline_frac": roof["pipeline"]["frac"],
+            "pipeline_bytes_per_pair": bp, "target": {"frac": 0.6, "ms_per_pair": target_ms,
+                                                      "met": m["ms"] <= target_ms},
+            "stages_ms_per_step": m["stages_ms_per_step"], "dominant_kernel": roof, "clocks": m["clocks"],
+            "f16": {"ms_per_pair": m16["ms"], "value": m16["value"], "ratio_to_plain": m16["value"] / m["value"],
+                    "agreement": agreement(m["out"], m16["out"]), "pipeline_frac": m16["roofline"]["pipeline"]["frac"],
+                    "stages_ms_per_step": m16["stages_ms_per_step"], "clocks": m16["clocks"]}}
+
+
+def f16_record(bench, plain):
+    """The FP16 form of the same workload as the line's plain run."""
+    import rtstereo_gb300 as R
+    m = bench.measure(plain["name"], "f16")
+    rec = {"value": m["value"], "unit": "MDE/s", "ms_per_step": m["ms"], "ratio_to_plain": m["value"] / plain["value"],
+           "e2e": m["e2e"], "agreement": agreement(plain["out"], m["out"]), "roofline": m["roofline"],
+           "stages_ms_per_step": m["stages_ms_per_step"], "clocks": m["clocks"]}
+    if plain["ag"] == 2:
+        rec["cost_error_vs_f64"] = aw_cost_error_vs_f64(bench.ctx, R, m["params"], plain["params"], *plain["imgs"])
+    return rec
+
+
+def run_ours(args, rank, world):
+    import torch
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    dist_init(world)
+    bench = Bench(dev, world, args.steps, args.warmup)
+    m = bench.measure(args.workload, args.precision)
+    extra = {}
+    # the other north-star figures ride on the default line (one GPU): the FP16 form,
+    # the 1920x1080 cross-based pipeline, and the serving loop
+    if world == 1 and args.workload == DEFAULT and args.precision == "f32" and not args.no_extra:
+        peaks, _ = measured_peaks()
+        extra["f16"] = f16_record(bench, m)
+        extra["c2_cross_1080p"] = c2_cross_record(bench, peaks)
+        srv = serve_measure(bench.ctx, args.serve_rate, args.requests, args.budget_gb, args.max_batch,
+                            args.priority_pixels, "f16", world)
+        extra["serve"] = {k: srv[k] for k in ("value", "unit", "offered_per_s", "requests", "latency_target",
+                                              "latency_ms", "one_at_a_time", "config", "clocks")}
     if rank != 0:
         ranks_done(world)
         return
-
-    peaks, src = measured_peaks()
-    roof = roofline(stages, name, W, H, D, ag, peaks, src, p, ms)
-    line = {"metric": "MDE/s", "value": value, "unit": "MDE/s", "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f16" if prec else "f32",
+    line = {"metric": "MDE/s", "value": m["value"], "unit": "MDE/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": m["ms"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f16" if args.precision == "f16" else "f32",
             "data": "synthetic random-dot stereo pair (seeded, no dataset)",
-            "config": {"workload": name, "width": W, "height": H, "disp_range": D,
-                       "pipeline": "cost1=%d cost2=%d aggr=%d, both views + cross check" % (c1, c2, ag),
-                       "precision": args.precision, "l2": "flushed (256 MB write) before every timed step",
-                       "parallelism": f"replicas{world}"},
-            "e2e": {"value": world * mde_pair / (e2e_ms / 1e3), "unit": "MDE/s", "ms_per_step": e2e_ms,
-                    "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "host_equals_device_result": agree},
-            "gpu_launches": launches, "wall_s": wall,
-            **({"f16_vs_f32_agreement": f16_agree} if f16_agree else {}),
-            "stages_ms_per_step": {k: v[1] / args.steps for k, v in stages.items()},
-            "roofline": roof, "clocks": clk.summary()}
+            "config": workload_config(args.workload, args.precision, world),
+            "e2e": m["e2e"], "gpu_launches": m["gpu_launches"], "wall_s": m["wall_s"],
+            "stages_ms_per_step": m["stages_ms_per_step"], "roofline": m["roofline"], "clocks": m["clocks"], **extra}
     if not args.no_cpu:
-        threads = 1
-        mde, dt, sample = cpu_sample(name, args.cpu_rows, threads)
         import oracle
-        line["cpu_baseline"] = {"value": mde, "unit": "MDE/s", "cores": threads,
-                                "kind": "reference" if oracle.have_reference() else "port", "sample": sample,
+        cs = CpuSampler(args.workload, args.cpu_rows, 1)
+        try:
+            mde, dt = cs.run()
+        finally:
+            cs.close()
+        line["cpu_baseline"] = {"value": mde, "unit": "MDE/s", "cores": 1,
+                                "kind": "reference" if oracle.have_reference() else "port", "sample": cs.sample,
                                 "seconds": dt}
     print(json.dumps(line), flush=True)
     ranks_done(world)
@@ -678,7 +786,7 @@ NCU_BYTES_PER_ENTRY = {("cross_vert_wta", 0): 4.16, ("cross_hseg", 0): 4.00,
 NCU_AW_BYTES = {(640, 480, 64): 85.61e6}
 
 
-def roofline(stages, name, W, H, D, ag, peaks, src, p, ms_pair=None):
+def roofline(stages, name, W, H, D, ag, peaks, src, p, ms_pair=None, sms=152):
     """Dominant kernel: algorithmic work per launch / its CUDA-event time, against
     the measured peak; traffic = DRAM bytes per launch from ncu."""
     if not stages:
@@ -688,19 +796,23 @@ def roofline(stages, name, W, H, D, ag, peaks, src, p, ms_pair=None):
     per_launch_ms = total_ms / max(1, launches)
     E = W * H * D  # entries per view
     if kname == "aw_wta":
-        # one launch = one view; 4 FP32 operations per tap per entry (w = wR*wT, sum w,
-        # C*w, sum), the reference's order, unfused
+        # one launch = one view.  Per tap per entry the plain form issues 4 FP32-pipe
+        # operations (w = wR*wT, sum w, C*w, sum: the reference's order, unfused), the
+        # FP16 form 3 (the last two as one fused multiply-add)
         taps = (2 * p.aw_rad + 1) ** 2
-        flops = 4.0 * taps * E
-        achieved = flops / (per_launch_ms / 1e3) / 1e12
+        ops_per_tap = 3 if p.precision else 4
+        ops = float(ops_per_tap * taps * E)
+        achieved = ops / (per_launch_ms / 1e3) / 1e12
         mhz = peaks.get("sm_max_mhz", 2070.0)
-        peak = 152 * 128 * mhz * 1e6 / 1e12  # one FP32 op per lane per clock (unfused ops)
+        peak = sms * 128 * mhz * 1e6 / 1e12  # one FP32 operation per lane per clock
         traffic = NCU_AW_BYTES.get((W, H, D)) if not p.precision else None
-        return {"bound": "fp32", "kernel": "k_aw_wta" if p.precision else "k_aw_wta_pipe", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+        kern = "k_aw_wta_pipe" if (not p.precision or D % 8 == 0) else "k_aw_wta"
+        return {"bound": "fp32", "kernel": kern, "achieved": achieved, "peak": peak, "unit": "T FP32-pipe op/s",
                 "frac": achieved / peak, "traffic": traffic, "launches": launches, "ms_per_launch": per_launch_ms,
-                "flop_per_launch": flops,
-                "peak_source": f"FP32 pipe, unfused operations: 152 SMs x 128 lanes x {mhz:.0f} MHz "
-                               f"({src} max clock); no tensor-core or HBM bound applies (DRAM < 1% busy)"}
+                "ops_per_launch": ops, "ops_per_tap": ops_per_tap,
+                "peak_source": f"FP32 pipe: {sms} SMs (device attribute) x 128 lanes x {mhz:.0f} MHz "
+                               f"({src} max clock), one operation per lane per clock; no tensor-core or HBM "
+                               f"bound applies (DRAM < 1% busy)"}
     # HBM stage model (one launch = both views): the cost volume crosses HBM four
     # times per view at S bytes an entry; the row-segment kernel owns the first two
     # crossings (written by matching and combining, read by aggregation), the
@@ -743,6 +855,10 @@ def main():
     ap.add_argument("--cpu-rows", type=int, default=None,
                     help="rows per CPU strip (default 48 for the 1-thread baseline, 24 for --impl reference)")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-extra", action="store_true",
+                    help="default workload: skip the f16 / c2_cross_1080p / serve sub-records")
+    ap.add_argument("--serve-rate", type=float, default=600.0,
+                    help="offered rate (pairs/s) of the serve sub-record of the default line")
     args = ap.parse_args()
     if args.cpu_rows is None:
         args.cpu_rows = 24 if args.impl == "reference" else 48

@@ -262,7 +262,13 @@ rts_status rts_server_submit(rts_server *s, const rts_pair *pair, const rts_para
 /* 1 done, 0 pending, <0 an error status (negated) */
 int rts_server_poll(rts_server *s, uint64_t ticket);
 rts_status rts_server_wait(rts_server *s, uint64_t ticket, double timeout_ms, rts_request_stats *stats);
+/* A pending request is dropped at once; a running one when its batch leaves
+ * the device.  wait / poll then report RTS_ERR_CANCELLED for the ticket (for the
+ * 4096 most recently cancelled tickets). */
 rts_status rts_server_cancel(rts_server *s, uint64_t ticket);
+/* Requests the server still holds: pending, running, or finished and not yet
+ * collected by rts_server_wait (cancelled ones are not held). */
+long rts_server_tracked(rts_server *s);
 /* Drives admission and completion; call from the submitting thread or let
  * rts_server_wait drive it. */
 rts_status rts_server_progress(rts_server *s);

@@ -64,7 +64,16 @@ _ORACLE_SIGS = {
     "orc64_ncc": [_p, _p, _p, _i, _i, _i, _i, _i],
     "orc64_convolve": [_p, _p, _p, _i, _i, _i, _i],
     "orc_pipeline": [_p, _i, _i, _p, _p, _p, _p, _p, _p, _p, _p, _p, _p],
+    "orc_compute_weights_rows": [_p, _p, _p, _f, _i, _i, _i, _i, _i],
+    "orc_aw_l2r_rows": [_p, _p, _p, _p, _i, _i, _i, _i, _i, _i],
+    "orc_view_cost": [_p, _i, _i, _p, _p, _p, _p, _p],
+    "orc_set_threads": [_i],
+    "orc_threads": [],
+    "orc_synth_pair": [C.c_uint64, _i, _i, _i, _i, _i, _f, _i, _p, _p, _p],
+    "orc_gray_to_rgb": [_p, _p, _i, _i],
+    "orc_rgb_to_lab": [_p, _p, _i, _i],
 }
+_INT_RESULT = ("orc_pipeline", "orc64_aw_l2r_pre", "orc_view_cost", "orc_threads", "orc_synth_pair")
 
 
 class OrcParams(C.Structure):
@@ -89,13 +98,16 @@ class OrcParams(C.Structure):
 
 
 def build(force: bool = False) -> None:
-    """Compile the restatement with gcc (same flags as oracle/Makefile)."""
+    """Compile the restatement with gcc (same flags as oracle/Makefile): with
+    OpenMP where the compiler has it (row loops on all host threads), else
+    serial; the results are the same either way."""
     src = os.path.join(HERE, "rts_oracle.c")
     if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < max(
             os.path.getmtime(src), os.path.getmtime(os.path.join(HERE, "rts_oracle.h"))):
         tmp = LIB_PATH + ".tmp"
-        subprocess.run(["gcc", "-O2", "-std=c11", "-fPIC", "-shared", "-ffp-contract=off", "-o", tmp, src, "-lm"],
-                       check=True, capture_output=True)
+        base = ["gcc", "-O2", "-std=c11", "-fPIC", "-shared", "-ffp-contract=off", "-o", tmp, src, "-lm"]
+        if subprocess.run(base[:1] + ["-fopenmp"] + base[1:], capture_output=True).returncode != 0:
+            subprocess.run(base, check=True, capture_output=True)
         os.replace(tmp, LIB_PATH)
 
 
@@ -103,7 +115,7 @@ def _bind(lib, sigs):
     for name, args in sigs.items():
         fn = getattr(lib, name)
         fn.argtypes = args
-        fn.restype = _i if name in ("orc_pipeline", "orc64_aw_l2r_pre") else None
+        fn.restype = _i if name in _INT_RESULT else None
     return lib
 
 
@@ -282,6 +294,24 @@ def aw_l2r(wref, wtar, cost, rad):
     return out
 
 
+def aw_l2r_rows(lab_ref, lab_tar, cost, rows, rad, gamma_s, gamma_p):
+    """Rows `rows` of the left-to-right adaptive-weight aggregation of the whole
+    volume `cost`, with only those rows' weights made (a 1920x1080 image's full
+    weight arrays would take 9 GB each).  Returns [len(rows)][W][D]."""
+    H, W, D = cost.shape
+    cost = np.ascontiguousarray(cost, np.float32)
+    pw = prox_weight(gamma_p, rad)
+    area = pw.size
+    out = np.empty((len(rows), W, D), np.float32)
+    for i, y in enumerate(rows):
+        wr = np.empty((W, area), np.float32)
+        wt = np.empty((W, area), np.float32)
+        lib().orc_compute_weights_rows(ptr(wr), ptr(pw), ptr(lab_ref), gamma_s, H, W, rad, int(y), 1)
+        lib().orc_compute_weights_rows(ptr(wt), ptr(pw), ptr(lab_tar), gamma_s, H, W, rad, int(y), 1)
+        lib().orc_aw_l2r_rows(ptr(wr), ptr(wt), ptr(cost), ptr(out[i]), H, W, D, rad, int(y), 1)
+    return out
+
+
 def aw_r2l(wref, wtar, cost, rad, inplace=False):
     H, W, D = cost.shape
     if inplace:
@@ -391,6 +421,53 @@ def pipeline(p: OrcParams, lgray, rgray, lrgb, rrgb, llab=None, rlab=None, want_
     if rc != 0:
         raise RuntimeError("oracle pipeline failed (bad parameters or out of memory)")
     return dl, dr, mk, cost
+
+
+def view_cost(p: OrcParams, lgray, rgray, lrgb, rrgb):
+    """The left view's matching cost volume (cost1, cost2 combined), [H][W][D]."""
+    H, W = lgray.shape
+    out = np.empty((H, W, p.D), np.float32)
+    if lib().orc_view_cost(C.byref(p), H, W, ptr(lgray), ptr(rgray), ptr(lrgb), ptr(rrgb), ptr(out)) != 0:
+        raise RuntimeError("oracle view cost failed")
+    return out
+
+
+def set_threads(n: int) -> None:
+    """Host threads for the oracle's row loops (n <= 0: all processors)."""
+    lib().orc_set_threads(int(n))
+
+
+def threads() -> int:
+    return int(lib().orc_threads())
+
+
+def synth_pair(seed: int, width: int, height: int, max_disp: int, n_rects: int, n_planes: int = 0,
+               sigma: float = 2.0, bg_disp: int = 4):
+    """Seeded random-dot pair (left_gray, right_gray, gt_disp): the library's
+    generator restated, for CPU runs that must not load the library."""
+    L = np.empty((height, width), np.uint8)
+    R = np.empty((height, width), np.uint8)
+    G = np.empty((height, width), np.uint8)
+    if lib().orc_synth_pair(seed, width, height, max_disp, n_rects, n_planes, sigma, bg_disp, ptr(L), ptr(R),
+                            ptr(G)) != 0:
+        raise ValueError("orc_synth_pair: bad arguments")
+    return L, R, G
+
+
+def gray_to_rgb(g):
+    g = np.ascontiguousarray(g, np.uint8)
+    H, W = g.shape
+    out = np.empty((H, W, 3), np.uint8)
+    lib().orc_gray_to_rgb(ptr(g), ptr(out), W, H)
+    return out
+
+
+def rgb_to_lab(rgb):
+    rgb = np.ascontiguousarray(rgb, np.uint8)
+    H, W, _ = rgb.shape
+    out = np.empty((H, W, 3), np.uint8)
+    lib().orc_rgb_to_lab(ptr(rgb), ptr(out), W, H)
+    return out
 
 
 def ref_pipeline(p: OrcParams, lgray, rgray, lrgb, rrgb, llab=None, rlab=None):

@@ -19,6 +19,42 @@
 #include <stdlib.h>
 #include <string.h>
 
+/* Output rows of the out-of-place functions are independent, so their row
+ * loops may run on several host threads (OpenMP, when the build has it): every
+ * entry is still computed by one thread with the same operations in the same
+ * order, so the results do not depend on the thread count.  The in-place
+ * recurrences (orc_box_inplace, orc_aw_r2l, orc_disp_refinement) and the WTA
+ * winner carry stay serial. */
+#ifdef _OPENMP
+#include <omp.h>
+#define ORC_PRAGMA(x) _Pragma(#x)
+#define ORC_PAR ORC_PRAGMA(omp parallel for schedule(dynamic, 1))
+#define ORC_PAR_IF(c) ORC_PRAGMA(omp parallel for schedule(dynamic, 1) if (c))
+#define ORC_PAR_FLAT ORC_PRAGMA(omp parallel for schedule(static))
+#define ORC_PAR_PIXELS ORC_PRAGMA(omp parallel for collapse(2) schedule(dynamic, 16))
+#else
+#define ORC_PAR_FLAT
+#define ORC_PAR_PIXELS
+#define ORC_PAR
+#define ORC_PAR_IF(c)
+#endif
+
+void orc_set_threads(int n) {
+#ifdef _OPENMP
+    omp_set_num_threads(n > 0 ? n : omp_get_num_procs());
+#else
+    (void)n;
+#endif
+}
+
+int orc_threads(void) {
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+
 const float orc_log5x5[25] = {
     0.0239f, 0.046f,   0.0499f,  0.046f,   0.0239f,
     0.046f,  0.0061f, -0.0923f,  0.0061f,  0.046f,
@@ -46,6 +82,7 @@ static inline int tar_col(int x, int d, int W, int dir) {
 
 /* seq/PixelBasedCost.cpp:13-37 pixelBasedL2R / pixelBasedR2L */
 void orc_ad_gray(const uint8_t *ref, const uint8_t *tar, float *cost, int D, int H, int W, int dir) {
+    ORC_PAR
     for (int y = 0; y < H; y++)
         for (int x = 0; x < W; x++) {
             long p = (long)y * W + x;
@@ -58,6 +95,7 @@ void orc_ad_gray(const uint8_t *ref, const uint8_t *tar, float *cost, int D, int
 
 /* seq/PixelBasedCost.cpp:39-69 pixelBasedCostL2R_Float / pixelBasedCostR2L_Float */
 void orc_ad_float(const float *ref, const float *tar, float *cost, int D, int H, int W, int dir) {
+    ORC_PAR
     for (int y = 0; y < H; y++)
         for (int x = 0; x < W; x++) {
             long p = (long)y * W + x;
@@ -75,6 +113,7 @@ void orc_ad_float(const float *ref, const float *tar, float *cost, int D, int H,
 void orc_ad_color(const uint8_t *ref, const uint8_t *tar, float *cost, int D, int H, int W,
                   int dir, int use_trunc, float trunc, int norm) {
     const float third = (float)1 / (float)3;
+    ORC_PAR
     for (int y = 0; y < H; y++)
         for (int x = 0; x < W; x++) {
             long p = (long)y * W + x;
@@ -96,6 +135,7 @@ void orc_ad_color(const uint8_t *ref, const uint8_t *tar, float *cost, int D, in
  * centre > neighbour (strict), neighbours wrap around both borders. */
 void orc_census(const uint8_t *img, uint8_t *bits, int hrad, int wrad, int H, int W) {
     int bw = 2 * wrad + 1, nb = (2 * hrad + 1) * bw;
+    ORC_PAR
     for (int y = 0; y < H; y++)
         for (int x = 0; x < W; x++) {
             long p = (long)y * W + x;
@@ -115,6 +155,7 @@ void orc_census(const uint8_t *img, uint8_t *bits, int hrad, int wrad, int H, in
 void orc_hamming(const uint8_t *bref, const uint8_t *btar, float *cost, int hrad, int wrad,
                  int H, int W, int D) {
     int nb = (2 * hrad + 1) * (2 * wrad + 1);
+    ORC_PAR
     for (int y = 0; y < H; y++)
         for (int x = 0; x < W; x++) {
             long p = (long)y * W + x;
@@ -131,6 +172,7 @@ void orc_hamming(const uint8_t *bref, const uint8_t *btar, float *cost, int hrad
 /* seq/RankFilter.cpp:11-35: 1 + #{neighbours strictly darker than the centre}
  * over a (2rad+1)^2 wrapped window, stored as unsigned char (wraps above 255). */
 void orc_rank(const uint8_t *img, uint8_t *out, int rad, int H, int W) {
+    ORC_PAR
     for (int y = 0; y < H; y++)
         for (int x = 0; x < W; x++) {
             long p = (long)y * W + x;
@@ -151,6 +193,7 @@ void orc_rank(const uint8_t *img, uint8_t *out, int rad, int H, int W) {
  * then |.| and min(.,255). */
 void orc_convolve(const uint8_t *img, float *out, const float *mask, int H, int W, int hrad, int wrad) {
     int mw = 2 * wrad + 1;
+    ORC_PAR
     for (int y = 0; y < H; y++)
         for (int x = 0; x < W; x++) {
             float acc = 0;
@@ -172,6 +215,7 @@ void orc_convolve(const uint8_t *img, float *out, const float *mask, int H, int 
  * the cell is left unwritten when den == 0 (:70-71). */
 void orc_ncc(const uint8_t *ref, const uint8_t *tar, float *cost, int D, int H, int W, int hrad, int wrad) {
     int area = (2 * hrad + 1) * (2 * wrad + 1);
+    ORC_PAR
     for (int y = 0; y < H; y++)
         for (int x = 0; x < W; x++) {
             long p = (long)y * W + x;
@@ -213,6 +257,7 @@ void orc_ncc(const uint8_t *ref, const uint8_t *tar, float *cost, int D, int H, 
 /* seq/CombineCost.cpp:11-25: c1 <- (1 - expf(-c1/l1)) + (1 - expf(-c2/l2)). */
 void orc_combine(float *c1, const float *c2, float lambda1, float lambda2, int H, int W, int D) {
     long n = (long)H * W * D;
+    ORC_PAR_FLAT
     for (long i = 0; i < n; i++) {
         float a = c1[i], b = c2[i];
         a = 1 - expf(-a / lambda1);
@@ -245,6 +290,7 @@ void orc_box_inplace(float *cost, int H, int W, int D, int rad) {
  * This is the contract of the GPU machine aggregation. */
 void orc_box(const float *cost, float *out, int H, int W, int D, int rad) {
     int area = (2 * rad + 1) * (2 * rad + 1);
+    ORC_PAR
     for (int y = 0; y < H; y++)
         for (int x = 0; x < W; x++)
             for (int d = 0; d < D; d++) {
@@ -288,10 +334,11 @@ static int arm_length(const uint8_t *rgb, long centre, long step, int room, int 
  * insertion and the middle one taken. */
 void orc_median(const uint8_t *img, uint8_t *out, int H, int W, int ch, int k) {
     int r = k / 2, n = k * k;
-    uint8_t v[225];
+    ORC_PAR
     for (int y = 0; y < H; y++)
         for (int x = 0; x < W; x++)
             for (int c = 0; c < ch; c++) {
+                uint8_t v[225];
                 int m = 0;
                 for (int dy = -r; dy <= r; dy++)
                     for (int dx = -r; dx <= r; dx++) {
@@ -309,6 +356,7 @@ void orc_median(const uint8_t *img, uint8_t *out, int H, int W, int ch, int k) {
 /* seq/CrossBasedAggregation.cpp:102-115 findCross: horz[2p]=left, horz[2p+1]=right,
  * vert[2p]=top, vert[2p+1]=bottom. */
 void orc_find_cross(const uint8_t *rgb, int *horz, int *vert, int H, int W, int arm_len, int tau) {
+    ORC_PAR
     for (int y = 0; y < H; y++)
         for (int x = 0; x < W; x++) {
             long p = (long)y * W + x;
@@ -321,6 +369,7 @@ void orc_find_cross(const uint8_t *rgb, int *horz, int *vert, int H, int W, int 
 
 /* seq/CrossBasedAggregation.cpp:117-125: in-place running sum along x per (y,d). */
 void orc_prefix_h(float *cost, int H, int W, int D) {
+    ORC_PAR
     for (int y = 0; y < H; y++)
         for (int x = 1; x < W; x++)
             for (int d = 0; d < D; d++) {
@@ -336,6 +385,7 @@ void orc_prefix_h(float *cost, int H, int W, int D) {
  * of the rows in top-to-bottom order is divided by the pixel count. */
 void orc_cross_aggr(const float *pre, float *out, const int *hr, const int *ht, const int *vr,
                     const int *vt, int H, int W, int D) {
+    ORC_PAR
     for (int y = 0; y < H; y++)
         for (int x = 0; x < W; x++) {
             long p = (long)y * W + x;
@@ -389,10 +439,17 @@ static inline float lab_dist(int l0, int l1, int a0, int a1, int b0, int b1) {
 /* seq/AdaptiveWeightAggregation.cpp:33-71: w[p][k] = pw[k]*expf(-|Lab(p)-Lab(q)|/gamma_s),
  * 0 where q falls outside the image (no wrap). */
 void orc_compute_weights(float *w, const float *pw, const uint8_t *lab, float gamma_s, int H, int W, int rad) {
+    orc_compute_weights_rows(w, pw, lab, gamma_s, H, W, rad, 0, H);
+}
+
+/* The weights of the pixels of rows y0 .. y0+nrows-1 only, into w[(y-y0)*W+x][k]. */
+void orc_compute_weights_rows(float *w, const float *pw, const uint8_t *lab, float gamma_s, int H, int W, int rad,
+                              int y0, int nrows) {
     int edge = 2 * rad + 1, area = edge * edge;
-    for (int y = 0; y < H; y++)
+    ORC_PAR_PIXELS
+    for (int y = y0; y < y0 + nrows; y++)
         for (int x = 0; x < W; x++) {
-            long p = (long)y * W + x;
+            long p = (long)y * W + x, pw_ = (long)(y - y0) * W + x;
             const uint8_t *c = lab + 3 * p;
             int k = 0;
             for (int dy = -rad; dy <= rad; dy++) {
@@ -405,7 +462,7 @@ void orc_compute_weights(float *w, const float *pw, const uint8_t *lab, float ga
                         float dist = lab_dist(c[0], q[0], c[1], q[1], c[2], q[2]);
                         v = pw[k] * expf(-dist / gamma_s);
                     }
-                    w[k + (long)area * p] = v;
+                    w[k + (long)area * pw_] = v;
                 }
             }
         }
@@ -414,12 +471,21 @@ void orc_compute_weights(float *w, const float *pw, const uint8_t *lab, float ga
 /* seq/AdaptiveWeightAggregation.cpp:73-111: out = sum_k wR[p][k] wT[p-d][k] C[q_k,d]
  * / sum_k wR wT; q_k wraps in x and y, the target pixel p-d wraps in x. */
 void orc_aw_l2r(const float *wref, const float *wtar, const float *cost, float *out, int H, int W, int D, int rad) {
+    orc_aw_l2r_rows(wref, wtar, cost, out, H, W, D, rad, 0, H);
+}
+
+/* Rows y0 .. y0+nrows-1 of orc_aw_l2r: the weights are those of
+ * orc_compute_weights_rows over the same rows, `out` holds those rows, `cost`
+ * is the whole volume. */
+void orc_aw_l2r_rows(const float *wref, const float *wtar, const float *cost, float *out, int H, int W, int D,
+                     int rad, int y0, int nrows) {
     int edge = 2 * rad + 1, area = edge * edge;
-    for (int y = 0; y < H; y++)
+    ORC_PAR_PIXELS
+    for (int y = y0; y < y0 + nrows; y++)
         for (int x = 0; x < W; x++) {
-            long p = (long)y * W + x;
+            long p = (long)(y - y0) * W + x;
             for (int d = 0; d < D; d++) {
-                long t = (long)y * W + tar_col(x, d, W, ORC_L2R);
+                long t = (long)(y - y0) * W + tar_col(x, d, W, ORC_L2R);
                 float sw = 0, sc = 0;
                 int k = 0;
                 for (int dy = -rad; dy <= rad; dy++) {
@@ -444,6 +510,7 @@ void orc_aw_l2r(const float *wref, const float *wtar, const float *cost, float *
 static void aw_r2l_core(const float *wref, const float *wtar, const float *src, float *dst,
                         int H, int W, int D, int rad) {
     int edge = 2 * rad + 1, area = edge * edge;
+    ORC_PAR_IF(src != dst)
     for (int y = 0; y < H; y++)
         for (int x = 0; x < W; x++) {
             long p = (long)y * W + x;
@@ -510,10 +577,10 @@ void orc_cross_check(const uint8_t *dref, const uint8_t *dtar, uint8_t *mask, in
  * src; src == dst gives the reference's in-place behaviour (later pixels vote
  * with already-refined values). */
 static void refine_core(const uint8_t *src, uint8_t *dst, const int *horz, const int *vert, int H, int W, int D) {
-    int *hist = (int *)malloc(sizeof(int) * 256);
-    if (!hist) return;
+    ORC_PAR_IF(src != dst)
     for (int y = 0; y < H; y++)
         for (int x = 0; x < W; x++) {
+            int hist[256];
             long p = (long)y * W + x;
             int t = vert[2 * p], b = vert[2 * p + 1];
             memset(hist, 0, sizeof(int) * 256);
@@ -531,7 +598,6 @@ static void refine_core(const uint8_t *src, uint8_t *dst, const int *horz, const
                 if (hist[i] > best) { best = hist[i]; arg = i; }
             dst[p] = (uint8_t)arg;
         }
-    free(hist);
 }
 
 void orc_disp_refinement(uint8_t *disp, const int *horz, const int *vert, int H, int W, int D) {
@@ -552,6 +618,7 @@ void orc64_combine(const float *c1, const float *c2, double lambda1, double lamb
 
 void orc64_aw_l2r(const uint8_t *labr, const uint8_t *labt, const float *cost, double *out,
                   int H, int W, int D, int rad, double gamma_s, double gamma_p) {
+    ORC_PAR
     for (int y = 0; y < H; y++)
         for (int x = 0; x < W; x++) {
             long p = (long)y * W + x;
@@ -598,6 +665,7 @@ int orc64_aw_l2r_pre(const uint8_t *labr, const uint8_t *labt, const double *cos
     for (int pass = 0; pass < 2; pass++) {
         const uint8_t *lab = pass ? labt : labr;
         double *w = pass ? wt : wr;
+        ORC_PAR
         for (int y = 0; y < H; y++)
             for (int x = 0; x < W; x++) {
                 long p = (long)y * W + x, k = 0;
@@ -615,6 +683,7 @@ int orc64_aw_l2r_pre(const uint8_t *labr, const uint8_t *labt, const double *cos
                     }
             }
     }
+    ORC_PAR
     for (int y = 0; y < H; y++)
         for (int x = 0; x < W; x++) {
             long p = (long)y * W + x;
@@ -638,6 +707,7 @@ int orc64_aw_l2r_pre(const uint8_t *labr, const uint8_t *labt, const double *cos
 
 void orc64_ncc(const uint8_t *ref, const uint8_t *tar, double *cost, int D, int H, int W, int hrad, int wrad) {
     int area = (2 * hrad + 1) * (2 * wrad + 1);
+    ORC_PAR
     for (int y = 0; y < H; y++)
         for (int x = 0; x < W; x++) {
             long p = (long)y * W + x;
@@ -667,6 +737,7 @@ void orc64_ncc(const uint8_t *ref, const uint8_t *tar, double *cost, int D, int 
 
 void orc64_convolve(const uint8_t *img, double *out, const float *mask, int H, int W, int hrad, int wrad) {
     int mw = 2 * wrad + 1;
+    ORC_PAR
     for (int y = 0; y < H; y++)
         for (int x = 0; x < W; x++) {
             double acc = 0;
@@ -735,6 +806,23 @@ static int one_cost(const orc_params *p, int which, int trunc_ad, int H, int W, 
     return -1;
 }
 
+/* The matching cost of one view (seq/Main.cpp:180-234): cost1 (truncated colour
+ * AD when cost1 is AD in a cross-based run), and cost2 combined into it. */
+int orc_view_cost(const orc_params *p, int H, int W, const uint8_t *rg, const uint8_t *tg, const uint8_t *rc,
+                  const uint8_t *tc, float *cost) {
+    if (one_cost(p, p->cost1, p->aggr == 3, H, W, rg, tg, rc, tc, cost)) return -1;
+    if (!p->cost2) return 0;
+    long ne = (long)H * W * p->D;
+    float *c2 = (float *)malloc(ne * sizeof(float));
+    if (!c2 || one_cost(p, p->cost2, 0, H, W, rg, tg, rc, tc, c2)) {
+        free(c2);
+        return -1;
+    }
+    orc_combine(cost, c2, p->lambda1, p->lambda2, H, W, p->D);
+    free(c2);
+    return 0;
+}
+
 /* ra / ta: the images the cross arms are found on (the colour images, or
  * their median-filtered copies) */
 static int one_view(const orc_params *p, int H, int W, const uint8_t *rg, const uint8_t *tg,
@@ -742,14 +830,9 @@ static int one_view(const orc_params *p, int H, int W, const uint8_t *rg, const 
                     const uint8_t *ra, const uint8_t *ta, uint8_t *disp, float *cost_out) {
     long np = (long)H * W, ne = np * p->D;
     int D = p->D, rc_ = -1;
-    float *c1 = (float *)malloc(ne * sizeof(float)), *c2 = NULL, *c3 = NULL;
+    float *c1 = (float *)malloc(ne * sizeof(float)), *c3 = NULL;
     if (!c1) return -1;
-    if (one_cost(p, p->cost1, p->aggr == 3, H, W, rg, tg, rc, tc, c1)) goto out;
-    if (p->cost2) {
-        c2 = (float *)malloc(ne * sizeof(float));
-        if (!c2 || one_cost(p, p->cost2, 0, H, W, rg, tg, rc, tc, c2)) goto out;
-        orc_combine(c1, c2, p->lambda1, p->lambda2, H, W, D);
-    }
+    if (orc_view_cost(p, H, W, rg, tg, rc, tc, c1)) goto out;
     float *fin = c1;
     if (p->aggr == 1) {
         if (p->box_inplace) orc_box_inplace(c1, H, W, D, p->box_rad);
@@ -789,7 +872,7 @@ static int one_view(const orc_params *p, int H, int W, const uint8_t *rg, const 
     if (cost_out) memcpy(cost_out, fin, ne * sizeof(float));
     rc_ = 0;
 out:
-    free(c1); free(c2); free(c3);
+    free(c1); free(c3);
     return rc_;
 }
 
@@ -850,4 +933,120 @@ int orc_pipeline(const orc_params *p, int H, int W,
     free(buf);
     free(med);
     return rc;
+}
+
+/* ------------------------------------------------------------------------- */
+/* Synthetic inputs for the CPU legs that must not load the product library   */
+/* (the timed reference arm).  The same generator as the library's            */
+/* rts_synth_pair / rts_gray_to_rgb / rts_rgb_to_lab: xoshiro256** seeded by   */
+/* splitmix64, 3x3 box-smoothed uniform texture, rectangles and slanted planes */
+/* of constant disparity, Box-Muller noise, rounding half away from zero, and */
+/* the CIE L*a*b* formulas (sRGB, D65) with 8-bit scaling.  The reference has */
+/* no generator; tests/test_oracle_synth.py checks the two bit for bit.       */
+
+typedef struct { uint64_t s[4]; } orc_rng;
+
+static uint64_t rng_rotl(uint64_t x, int k) { return (x << k) | (x >> (64 - k)); }
+
+static void rng_seed(orc_rng *r, uint64_t seed) {
+    uint64_t z = seed;
+    for (int i = 0; i < 4; i++) {
+        z += 0x9e3779b97f4a7c15ull;
+        uint64_t x = z;
+        x = (x ^ (x >> 30)) * 0xbf58476d1ce4e5b9ull;
+        x = (x ^ (x >> 27)) * 0x94d049bb133111ebull;
+        r->s[i] = x ^ (x >> 31);
+    }
+}
+
+static uint64_t rng_next(orc_rng *r) {
+    uint64_t *s = r->s;
+    const uint64_t res = rng_rotl(s[1] * 5, 7) * 9, t = s[1] << 17;
+    s[2] ^= s[0];
+    s[3] ^= s[1];
+    s[1] ^= s[2];
+    s[0] ^= s[3];
+    s[2] ^= t;
+    s[3] = rng_rotl(s[3], 45);
+    return res;
+}
+
+static int rng_below(orc_rng *r, int n) { return (int)((rng_next(r) >> 11) % (uint64_t)n); }
+static double rng_unit(orc_rng *r) { return ((rng_next(r) >> 11) + 1) * (1.0 / 9007199254740992.0); }
+static double rng_gauss(orc_rng *r) {
+    const double u1 = rng_unit(r), u2 = rng_unit(r);
+    return sqrt(-2.0 * log(u1)) * cos(6.283185307179586 * u2);
+}
+static int round_half_away(double v) { return v < 0 ? -(int)floor(-v + 0.5) : (int)floor(v + 0.5); }
+static int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
+
+int orc_synth_pair(uint64_t seed, int W, int H, int max_disp, int n_rects, int n_planes, float sigma, int bg_disp,
+                   uint8_t *left, uint8_t *right, uint8_t *gt) {
+    if (W <= 0 || H <= 0 || max_disp <= 0 || max_disp > 256 || !left || !right || n_rects < 0 || n_planes < 0)
+        return -1;
+    orc_rng rng;
+    rng_seed(&rng, seed);
+    const long np = (long)W * H;
+    uint8_t *raw = (uint8_t *)malloc(np), *d = (uint8_t *)malloc(np);
+    if (!raw || !d) { free(raw); free(d); return -1; }
+    for (long i = 0; i < np; i++) raw[i] = (uint8_t)(rng_next(&rng) >> 56);
+    for (int y = 0; y < H; y++)
+        for (int x = 0; x < W; x++) {
+            int s = 0;
+            for (int dy = -1; dy <= 1; dy++)
+                for (int dx = -1; dx <= 1; dx++)
+                    s += raw[(long)clampi(y + dy, 0, H - 1) * W + clampi(x + dx, 0, W - 1)];
+            left[(long)y * W + x] = (uint8_t)((s + 4) / 9);
+        }
+    memset(d, clampi(bg_disp, 0, max_disp - 1), np);
+    for (int i = 0; i < n_rects; i++) {
+        const int rw = 1 + rng_below(&rng, W / 3 > 1 ? W / 3 : 1), rh = 1 + rng_below(&rng, H / 3 > 1 ? H / 3 : 1);
+        const int x0 = rng_below(&rng, W), y0 = rng_below(&rng, H), dv = rng_below(&rng, max_disp);
+        for (int y = y0; y < y0 + rh && y < H; y++)
+            for (int x = x0; x < x0 + rw && x < W; x++) d[(long)y * W + x] = (uint8_t)dv;
+    }
+    for (int i = 0; i < n_planes; i++) {
+        const int rw = 1 + rng_below(&rng, W / 2 > 1 ? W / 2 : 1), rh = 1 + rng_below(&rng, H / 2 > 1 ? H / 2 : 1);
+        const int x0 = rng_below(&rng, W), y0 = rng_below(&rng, H);
+        const double a = rng_below(&rng, max_disp);
+        const double b = (rng_unit(&rng) - 0.5) * 2.0 * (double)max_disp / (double)W;
+        const double c = (rng_unit(&rng) - 0.5) * 2.0 * (double)max_disp / (double)H;
+        for (int y = y0; y < y0 + rh && y < H; y++)
+            for (int x = x0; x < x0 + rw && x < W; x++)
+                d[(long)y * W + x] = (uint8_t)clampi(round_half_away(a + b * (x - x0) + c * (y - y0)), 0, max_disp - 1);
+    }
+    for (int y = 0; y < H; y++)
+        for (int x = 0; x < W; x++) {
+            const int dv = d[(long)y * W + x];
+            const double v = left[(long)y * W + clampi(x + dv, 0, W - 1)] + (sigma > 0 ? sigma * rng_gauss(&rng) : 0.0);
+            right[(long)y * W + x] = (uint8_t)clampi(round_half_away(v), 0, 255);
+        }
+    if (gt) memcpy(gt, d, np);
+    free(raw);
+    free(d);
+    return 0;
+}
+
+void orc_gray_to_rgb(const uint8_t *gray, uint8_t *rgb, int W, int H) {
+    const long np = (long)W * H;
+    for (long i = 0; i < np; i++) rgb[3 * i] = rgb[3 * i + 1] = rgb[3 * i + 2] = gray[i];
+}
+
+static double srgb_to_linear(double c) { return c <= 0.04045 ? c / 12.92 : pow((c + 0.055) / 1.055, 2.4); }
+static double lab_f(double t) { return t > 216.0 / 24389.0 ? cbrt(t) : (24389.0 / 27.0 * t + 16.0) / 116.0; }
+
+void orc_rgb_to_lab(const uint8_t *rgb, uint8_t *lab, int W, int H) {
+    const long np = (long)W * H;
+    for (long i = 0; i < np; i++) {
+        const double r = srgb_to_linear(rgb[3 * i] / 255.0), g = srgb_to_linear(rgb[3 * i + 1] / 255.0),
+                     b = srgb_to_linear(rgb[3 * i + 2] / 255.0);
+        const double X = (0.4124564 * r + 0.3575761 * g + 0.1804375 * b) / 0.95047;
+        const double Y = 0.2126729 * r + 0.7151522 * g + 0.0721750 * b;
+        const double Z = (0.0193339 * r + 0.1191920 * g + 0.9503041 * b) / 1.08883;
+        const double fx = lab_f(X), fy = lab_f(Y), fz = lab_f(Z);
+        const double L = 116.0 * fy - 16.0, A = 500.0 * (fx - fy), B = 200.0 * (fy - fz);
+        lab[3 * i] = (uint8_t)clampi(round_half_away(L * 255.0 / 100.0), 0, 255);
+        lab[3 * i + 1] = (uint8_t)clampi(round_half_away(A + 128.0), 0, 255);
+        lab[3 * i + 2] = (uint8_t)clampi(round_half_away(B + 128.0), 0, 255);
+    }
 }

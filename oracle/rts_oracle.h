@@ -47,6 +47,11 @@ void orc_cross_aggr(const float *pre, float *out, const int *hr, const int *ht, 
 void orc_prox_weight(float *pw, float gamma_p, int rad);
 void orc_compute_weights(float *w, const float *pw, const uint8_t *lab, float gamma_s, int H, int W, int rad);
 void orc_aw_l2r(const float *wref, const float *wtar, const float *cost, float *out, int H, int W, int D, int rad);
+/* the same two steps for rows y0 .. y0+nrows-1 only (weights and output hold those rows) */
+void orc_compute_weights_rows(float *w, const float *pw, const uint8_t *lab, float gamma_s, int H, int W, int rad,
+                              int y0, int nrows);
+void orc_aw_l2r_rows(const float *wref, const float *wtar, const float *cost, float *out, int H, int W, int D,
+                     int rad, int y0, int nrows);
 void orc_aw_r2l(const float *wref, const float *wtar, float *cost, int H, int W, int D, int rad);
 /* out-of-place forms of the two in-place functions (the GPU contract) */
 void orc_aw_r2l_oop(const float *wref, const float *wtar, const float *cost, float *out, int H, int W, int D, int rad);
@@ -92,6 +97,23 @@ int orc_pipeline(const orc_params *p, int H, int W,
                  const uint8_t *lrgb, const uint8_t *rrgb,
                  const uint8_t *llab, const uint8_t *rlab,
                  uint8_t *disp_left, uint8_t *disp_right, uint8_t *mask, float *cost_out);
+
+/* One view's matching cost volume (cost1, and cost2 combined into it), as the
+ * pipeline makes it.  Returns 0, or -1 on allocation failure. */
+int orc_view_cost(const orc_params *p, int H, int W, const uint8_t *rg, const uint8_t *tg, const uint8_t *rc,
+                  const uint8_t *tc, float *cost);
+
+/* Host threads for the row loops (n <= 0: all processors); 1 when built without OpenMP. */
+void orc_set_threads(int n);
+int orc_threads(void);
+
+/* Seeded random-dot pairs and colour conversions, the same generator as the
+ * library's rts_synth_pair / rts_gray_to_rgb / rts_rgb_to_lab (the CPU legs
+ * that must not load the library make their inputs with these). */
+int orc_synth_pair(uint64_t seed, int W, int H, int max_disp, int n_rects, int n_planes, float sigma, int bg_disp,
+                   uint8_t *left, uint8_t *right, uint8_t *gt);
+void orc_gray_to_rgb(const uint8_t *gray, uint8_t *rgb, int W, int H);
+void orc_rgb_to_lab(const uint8_t *rgb, uint8_t *lab, int W, int H);
 
 /* the 5x5 LoG mask of the reference driver (seq/Main.cpp:113-117) */
 extern const float orc_log5x5[25];

@@ -383,6 +383,10 @@ class Server:
     def cancel(self, ticket) -> int:
         return int(self._lib.rts_server_cancel(self.h, ticket))
 
+    def tracked(self) -> int:
+        """Requests the server still holds (pending, running, or not yet waited for)."""
+        return int(self._lib.rts_server_tracked(self.h))
+
     def wait(self, ticket, timeout_ms: float = 60000.0):
         """Blocks until done; returns (submit_ms, start_ms, done_ms)."""
         st = RequestStats()

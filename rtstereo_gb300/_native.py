@@ -108,6 +108,7 @@ SIGNATURES = {
     "rts_server_wait": (i, [p, u64, d, C.POINTER(RequestStats)]),
     "rts_server_cancel": (i, [p, u64]),
     "rts_server_progress": (i, [p]),
+    "rts_server_tracked": (C.c_long, [p]),
     "rts_synth_pair": (i, [u64, i, i, i, i, i, f, i, p, p, p]),
     "rts_gray_to_rgb": (None, [p, p, i, i]),
     "rts_rgb_to_lab": (None, [p, p, i, i]),

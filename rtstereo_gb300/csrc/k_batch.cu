@@ -29,6 +29,7 @@
 
 #include "rts_fused.cuh"
 #include "rts_pipe.h"
+#include "rts_vert_ring.h"
 #include "rts_views.h"
 
 namespace rts {
@@ -339,14 +340,8 @@ __global__ void __launch_bounds__(kHsegW * 32, 8) k_hseg_views(ViewTable t, Cost
 constexpr int kVertW = 8;
 constexpr int kVertT = kVertW * 32;
 
-// ring depth in rows for arm length L.  A warp may write the next tick while a
-// slower warp still reads the previous step (one barrier per step): the newest
-// row then written is ra + 8 (T0 + s) - 1, the oldest row still read is
-// y0 + 8 (s - 1) - L, and with T0 = ceil((y0 - ra + 8 + L) / 8) they are at most
-// 2L + 22 rows apart (y0 - ra a multiple of 8, e.g. a strip at the image top).
-// The ring holds 2L + 23 rows or more, so the two never share a slot; a whole
-// number of ticks, even (two-row blocks never straddle the wrap).
-static int vert_depth(int L) { return 8 * ((2 * L + 23 + 7) / 8); }
+// ring depth and first ticks: rts_vert_ring.h (shared with the CPU check of
+// the ring arithmetic)
 
 // The ring accumulators: where a row lies in a disparity's arm, its segment is
 // added to the sum and its pixel count to the count, as predicated instructions
@@ -522,7 +517,7 @@ __device__ __forceinline__ void vert_item(const ViewDesc &V, int x, int y0, int 
     }
     __syncthreads();
     load_tick(0);
-    const int T0 = (y0 + 8 + L - ra + 7) >> 3;  // ticks the first step needs
+    const int T0 = vert_first_ticks(y0, ra, L);  // ticks the first step needs
     int i = 0;
     for (; i < T0 - 1; i++) ingest(i);
     const int nsteps = (y1 - y0 + 7) >> 3;
@@ -841,13 +836,14 @@ rts_status launch_cross_views(rts_ctx *c, const rts_params &p, const ViewTable &
         const int rk = rank ? p.rank_rad : -1;
         const int gr = std::max(hr, std::max(rk, 0)), gc = std::max(wr, std::max(rk, 0));
         const size_t smem = prep_smem(gr, gc, L);
-        auto go = [&](auto kern) {
-            cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        auto go = [&](auto kern) -> rts_status {
+            RTS_TRY(set_smem(c, kern, smem, "prep_views"));
             kern<<<grid(t.total[ST_PREP], 1, resident_blocks(kern, kPrepT, smem)), kPrepT, smem, s>>>(
                 t, hr, wr, L, p.cross_tau, want_code ? 1 : 0, rk, gr, gc);
+            return RTS_OK;
         };
-        if (grayrec == 1) go(k_prep_views<1>);
-        else go(k_prep_views<0>);
+        if (grayrec == 1) RTS_TRY(go(k_prep_views<1>));
+        else RTS_TRY(go(k_prep_views<0>));
         count_launch(c);
     }
     {
@@ -882,8 +878,10 @@ rts_status launch_cross_views(rts_ctx *c, const rts_params &p, const ViewTable &
         const size_t DMb = (size_t)32 * NCH;
         const size_t smem = (size_t)DEP * DMb * ((segk ? 4 : 8) + 2) + (size_t)DEP * 4 + DMb * 4;
         const int R = tune.vert_rows;
+        rts_status vs = RTS_OK;
         auto go = [&](auto kern) {
-            cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            vs = set_smem(c, kern, smem, "vert_views");
+            if (vs != RTS_OK) return;
             kern<<<grid(t.total[ST_VERT], 1, resident_blocks(kern, kVertT, smem)), kVertT, smem, s>>>(t, L, R, DEP,
                                                                                                    rcp);
         };
@@ -913,6 +911,7 @@ rts_status launch_cross_views(rts_ctx *c, const rts_params &p, const ViewTable &
             else RTS_VERT(float, 8);
         }
 #undef RTS_VERT
+        RTS_TRY(vs);
         count_launch(c);
     }
     {

@@ -758,9 +758,10 @@ rts_status aw_fused(rts_ctx *c, const rts_params &p, int H, int W, const void *v
                                          (size_t)(kAwTX + kAwDC - 1 + 2 * r));
     const dim3 grid((W + kAwTX - 1) / kAwTX, H);
     StageScope sc(c, "aw_wta");
-    auto go = [&](auto kern, auto *v) {
-        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    auto go = [&](auto kern, auto *v) -> rts_status {
+        RTS_TRY(set_smem(c, kern, smem, "aw_wta"));
         kern<<<grid, kAwThreads, smem, c->stream>>>(v, plr, plt, pw, g, raw, rl, cost_out, H, W, p.disp_range, e);
+        return RTS_OK;
     };
     // plain form: bit-exact float volume, the pipelined kernel; FP16 form: __half
     // volume and fused multiply-add
@@ -774,15 +775,15 @@ rts_status aw_fused(rts_ctx *c, const rts_params &p, int H, int W, const void *v
                sizeof(uint32_t) * 3 * ((size_t)(kAwTX + 2 * r) + (size_t)(kAwTX + kAwDC - 1 + 2 * r));
     };
     if (half && p.disp_range % 8 != 0) {
-        go(k_aw_wta<__half, false>, (const __half *)vol);
+        RTS_TRY(go(k_aw_wta<__half, false>, (const __half *)vol));
     } else if (half) {
         const size_t psmem = pipe_smem((size_t)kAwHPitch * 2);
-        cudaFuncSetAttribute(k_aw_wta_pipe<__half, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)psmem);
+        RTS_TRY(set_smem(c, k_aw_wta_pipe<__half, false>, psmem, "aw_wta_pipe"));
         k_aw_wta_pipe<__half, false><<<grid, kAwThreads, psmem, c->stream>>>((const __half *)vol, plr, plt, pw, g, raw,
                                                                              rl, cost_out, H, W, p.disp_range, e);
     } else {
         const size_t psmem = pipe_smem((size_t)kAwCPitch * 4);
-        cudaFuncSetAttribute(k_aw_wta_pipe<float, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)psmem);
+        RTS_TRY(set_smem(c, k_aw_wta_pipe<float, true>, psmem, "aw_wta_pipe"));
         k_aw_wta_pipe<float, true><<<grid, kAwThreads, psmem, c->stream>>>((const float *)vol, plr, plt, pw, g, raw,
                                                                            rl, cost_out, H, W, p.disp_range, e);
     }

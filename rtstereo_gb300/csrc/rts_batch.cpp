@@ -31,6 +31,7 @@
 #include <memory>
 #include <string>
 #include <unordered_map>
+#include <unordered_set>
 
 #include "rts_internal.h"
 #include "rts_pipe.h"
@@ -445,6 +446,11 @@ struct rts_server {
     std::vector<Batch> batches;
     std::unordered_map<uint64_t, std::unique_ptr<Request>> reqs;
     std::deque<uint64_t> queue;
+    // recently cancelled tickets whose entries are gone (off the device): wait and
+    // poll still report RTS_ERR_CANCELLED for them; the oldest are forgotten past
+    // kCancelMemory
+    std::unordered_set<uint64_t> cancelled;
+    std::deque<uint64_t> cancelled_order;
     uint64_t next_ticket = 1;
     int inflight = 0;
     int next_stream = 0;
@@ -463,6 +469,21 @@ size_t request_device_bytes(const Request &r) {
     const size_t np = (size_t)r.pair.width * r.pair.height;
     return ((r.in_bytes + 255) & ~size_t(255)) + ((3 * np + 255) & ~size_t(255)) +
            (r.params.median_ksize ? median_pair_bytes(r.pair) : 0);
+}
+
+constexpr size_t kCancelMemory = 4096;
+
+// Drops a cancelled request that is off the device and out of the queue; its
+// ticket is remembered as cancelled.
+void drop_cancelled(rts_server *s, uint64_t ticket) {
+    s->reqs.erase(ticket);
+    if (s->cancelled.insert(ticket).second) {
+        s->cancelled_order.push_back(ticket);
+        if (s->cancelled_order.size() > kCancelMemory) {
+            s->cancelled.erase(s->cancelled_order.front());
+            s->cancelled_order.pop_front();
+        }
+    }
 }
 
 void finish_batch(rts_server *s, Batch &bt) {
@@ -488,6 +509,7 @@ void finish_batch(rts_server *s, Batch &bt) {
         s->staging.put(r.h_in);
         r.h_in = r.h_out = nullptr;
         s->inflight--;
+        if (r.state == RQ_CANCELLED) drop_cancelled(s, tk);  // cancelled while running: nothing to deliver
     }
     s->pool.release(bt.arena, bt.arena_bytes);
     bt.arena = nullptr;
@@ -842,7 +864,7 @@ int rts_server_poll(rts_server *s, uint64_t ticket) {
     if (st != RTS_OK) return -(int)st;
     std::lock_guard<std::mutex> g(s->mu);
     auto it = s->reqs.find(ticket);
-    if (it == s->reqs.end()) return -(int)RTS_ERR_INVALID_ARG;
+    if (it == s->reqs.end()) return s->cancelled.count(ticket) ? -(int)RTS_ERR_CANCELLED : -(int)RTS_ERR_INVALID_ARG;
     switch (it->second->state) {
     case RQ_DONE: return 1;
     case RQ_CANCELLED: return -(int)RTS_ERR_CANCELLED;
@@ -856,13 +878,7 @@ rts_status rts_server_wait(rts_server *s, uint64_t ticket, double timeout_ms, rt
     const double t_end = s->now_ms() + timeout_ms;
     for (;;) {
         const int r = rts_server_poll(s, ticket);
-        if (r == -(int)RTS_ERR_CANCELLED) {
-            std::lock_guard<std::mutex> g(s->mu);
-            auto it = s->reqs.find(ticket);
-            if (it != s->reqs.end() && it->second->d_mem == nullptr)  // no longer on the device
-                s->reqs.erase(it);
-            return RTS_ERR_CANCELLED;
-        }
+        if (r == -(int)RTS_ERR_CANCELLED) return RTS_ERR_CANCELLED;  // the entry goes when it leaves the device
         if (r < 0) return (rts_status)(-r);
         if (r == 1) break;
         if (s->now_ms() > t_end) return RTS_ERR_TIMEOUT;
@@ -875,6 +891,12 @@ rts_status rts_server_wait(rts_server *s, uint64_t ticket, double timeout_ms, rt
     return RTS_OK;
 }
 
+long rts_server_tracked(rts_server *s) {
+    if (!s) return -1;
+    std::lock_guard<std::mutex> g(s->mu);
+    return (long)s->reqs.size();
+}
+
 rts_status rts_server_cancel(rts_server *s, uint64_t ticket) {
     if (!s) return RTS_ERR_INVALID_ARG;
     std::lock_guard<std::mutex> g(s->mu);
@@ -882,9 +904,12 @@ rts_status rts_server_cancel(rts_server *s, uint64_t ticket) {
     if (it == s->reqs.end()) return RTS_ERR_INVALID_ARG;
     Request &r = *it->second;
     if (r.state == RQ_PENDING) {
-        r.state = RQ_CANCELLED;  // skipped at admission
+        // never admitted: out of the queue and forgotten now
         s->staging.put(r.h_in);
         r.h_in = r.h_out = nullptr;
+        auto q = std::find(s->queue.begin(), s->queue.end(), ticket);
+        if (q != s->queue.end()) s->queue.erase(q);
+        drop_cancelled(s, ticket);
         return RTS_OK;
     }
     if (r.state == RQ_RUNNING) {

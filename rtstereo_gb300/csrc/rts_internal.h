@@ -122,6 +122,19 @@ struct StageScope {
     ~StageScope();
 };
 rts_status check_launch(rts_ctx *c, const char *what);
+// Opts `kern` into `smem` bytes of dynamic shared memory, checking the result
+// (a request above the device's opt-in limit fails here, with the kernel's name,
+// rather than later as a generic launch error).
+template <typename K> rts_status set_smem(rts_ctx *c, K kern, size_t smem, const char *what) {
+    int dev = 0, limit = 0;
+    RTS_CU(c, cudaGetDevice(&dev));
+    RTS_CU(c, cudaDeviceGetAttribute(&limit, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    if (smem > (size_t)limit)
+        return set_error(c, RTS_ERR_UNSUPPORTED, std::string(what) + ": " + std::to_string(smem) +
+                                                     " bytes of shared memory exceed the device's " +
+                                                     std::to_string(limit));
+    return cuda_check(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem), what);
+}
 
 // host-computed tables (glibc expf/sqrtf, same as the reference) ----------
 // combine LUT: T[v] = 1 - expf(-(float)v / lambda), v in [0, kCombineLut)

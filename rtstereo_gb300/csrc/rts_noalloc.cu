@@ -59,6 +59,9 @@ extern "C" rts_status rts_WTA_noalloc(const float *cost, uint8_t *winners, int r
     if (!cost || !winners) return RTS_ERR_INVALID_ARG;
     if (rdim <= 0 || cdim <= 0 || dispRange <= 0 || dispRange > kMaxDisp) return RTS_ERR_INVALID_ARG;
     if ((long)rdim * cdim > kNoAllocMaxPixels || rdim > kNoAllocMaxRows) return RTS_ERR_INVALID_ARG;
+    // an error left by earlier work on this thread is reported before any work of
+    // this call, so that the status after the launches is this call's own
+    if (cudaGetLastError() != cudaSuccess) return RTS_ERR_CUDA;
     void *base = nullptr;
     cudaError_t e = noalloc_scratch(&base);
     if (e != cudaSuccess) return e == cudaErrorNoDevice ? RTS_ERR_UNSUPPORTED : RTS_ERR_CUDA;
@@ -68,6 +71,7 @@ extern "C" rts_status rts_WTA_noalloc(const float *cost, uint8_t *winners, int r
     // the row summaries must start at -1 on every call (the array keeps the last call's contents)
     if (cudaMemsetAsync(row_last, 0xff, (size_t)rdim * sizeof(int), s) != cudaSuccess) return RTS_ERR_CUDA;
     launch_wta_local(s, cost, raw, row_last, rdim, cdim, dispRange, 0);
+    if (cudaGetLastError() != cudaSuccess) return RTS_ERR_CUDA;
     launch_wta_fill(s, raw, row_last, winners, rdim, cdim, 0);
     return cudaGetLastError() == cudaSuccess ? RTS_OK : RTS_ERR_CUDA;
 }

@@ -323,9 +323,8 @@ static rts_status view_fused(rts_ctx *c, const rts_params &p, int H, int W, cons
 
 rts_status run_view(rts_ctx *c, const rts_params &p, int H, int W, const ViewIn &v, uint8_t *disp, int mirror,
                     float *cost_out) {
-    // the FP16 form's final volume comes from its own (fused) kernel
-    if (p.aggr == RTS_AGGR_AW && fused_supported(p, H, W) && (!cost_out || p.precision == RTS_PREC_F16))
-        return view_fused(c, p, H, W, v, disp, mirror, cost_out);
+    // the fused kernel also writes the final volume when one is asked for
+    if (p.aggr == RTS_AGGR_AW && fused_supported(p, H, W)) return view_fused(c, p, H, W, v, disp, mirror, cost_out);
     return view_composed(c, p, H, W, v, disp, mirror, cost_out);
 }
 

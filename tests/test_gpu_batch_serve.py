@@ -2,6 +2,8 @@
 replay, autotuned tiles) and the serving loop (rts_server_*): every pair's
 result is the same as its single-pair pipeline run -- alone and in the mix --
 and the single-pair run is pinned to the oracle elsewhere."""
+import time
+
 import numpy as np
 import pytest
 
@@ -179,5 +181,18 @@ def test_server_cancel_while_held(ctx):
         for (L, Rr), D, outs in ((big[0], 64, oa), (big[1], 64, ob), (small[1], 32, os2)):
             for g, w in zip(outs, single(ctx, L, Rr, D, R.PREC_F16)):
                 assert bits_equal(g, w)
+        # every request was collected or cancelled: the server holds none
+        assert srv.tracked() == 0
+        # a request cancelled while it runs is dropped when its batch leaves the device
+        tc, _ = srv.submit(p(64), *big[0])
+        srv.progress()
+        assert srv.cancel(tc) == 0
+        t_end = time.time() + 10.0
+        while srv.tracked() and time.time() < t_end:
+            srv.progress()
+        assert srv.tracked() == 0
+        with pytest.raises(R.RtsError) as e:
+            srv.wait(tc)
+        assert e.value.status == 7  # RTS_ERR_CANCELLED, from the record of cancelled tickets
     finally:
         srv.close()

@@ -1,0 +1,166 @@
+"""GPU parity at the full sizes of the benchmark configurations, against the
+oracle (row-parallel on the host, same per-entry arithmetic):
+
+* 640x480, D=64, AD + census, adaptive weights 33x33, both views and the mask
+  (seq/AdaptiveWeightAggregation.cpp:73-111) -- the default benchmark pair;
+* 1920x1080, D=128: cross-based (AD + census, census alone, rank 7x7 + census,
+  LoG 5x5 + census), box 9x9, NCC 7x7 + box 9x9 (seq/CrossBasedAggregation.cpp:
+  127-169, seq/ConstBlockAggregation.cpp:11-34, seq/NCCDisparity.cpp:11-73);
+* 1920x1080, D=128 adaptive weights: the returned left cost volume on sampled
+  rows (the oracle's weights of a whole 1080p image would take 9 GB), and the
+  disparities against the arg-min of that volume;
+* one batch of 64 mixed pairs through rts_batch_run, each pair against the
+  oracle;
+* the FP16 form against the plain form: at least 99.5 % equal disparities.
+
+The GPU runs take the same entry point and the same autotuned full-size tiles
+as the benchmark (a cross-based pair gets gray images only, as there)."""
+import numpy as np
+import pytest
+
+from conftest import bits_equal
+
+pytestmark = pytest.mark.gpu
+
+# workload sizes and generator settings of the benchmark configurations
+C1 = dict(W=640, H=480, D=64, rects=12, planes=1, sigma=2.0, seed=0xC1)
+C2 = dict(W=1920, H=1080, D=128, rects=24, planes=2, sigma=3.0, seed=0xC2)
+
+
+def pair(cfg):
+    import rtstereo_gb300 as R
+    L, Rr, _ = R.synth_pair(cfg["seed"], cfg["W"], cfg["H"], cfg["D"], cfg["rects"], cfg["planes"], cfg["sigma"],
+                            min(4, cfg["D"] - 1))
+    return L, Rr
+
+
+def oracle_params(O, p):
+    return O.params(cost1=p.cost1, cost2=p.cost2, aggr=p.aggr, lambda1=p.lambda1, lambda2=p.lambda2, D=p.disp_range,
+                    census_hrad=p.census_hrad, census_wrad=p.census_wrad, rank_rad=p.rank_rad,
+                    ncc_hrad=p.ncc_hrad, ncc_wrad=p.ncc_wrad, box_rad=p.box_rad, aw_rad=p.aw_rad,
+                    aw_gamma_s=p.aw_gamma_s, aw_gamma_p=p.aw_gamma_p, cross_L=p.cross_arm, cross_tau=p.cross_tau,
+                    ad_trunc=p.ad_trunc, right_view=p.right_view, box_inplace=0)
+
+
+def assert_pair_equal(g, o, what):
+    assert bits_equal(g[0], o[0]), f"{what}: left disparity ({(g[0] != o[0]).sum()} pixels differ)"
+    assert bits_equal(g[1], o[1]), f"{what}: right disparity ({(g[1] != o[1]).sum()} pixels differ)"
+    assert bits_equal(g[2], o[2]), f"{what}: cross-check mask"
+
+
+def test_config1_adaptive_weights_640x480(ctx, oracle_mod):
+    import rtstereo_gb300 as R
+    O = oracle_mod
+    L, Rr = pair(C1)
+    Lc, Rc = R.gray_to_rgb(L), R.gray_to_rgb(Rr)
+    Ll, Rl = R.rgb_to_lab(Lc), R.rgb_to_lab(Rc)
+    p = R.params(cost1=1, cost2=3, aggr=2, disp_range=C1["D"])
+    g = ctx.pipeline(p, L, Rr, Lc, Rc, Ll, Rl)
+    o = O.pipeline(oracle_params(O, p), L, Rr, Lc, Rc, Ll, Rl)
+    assert_pair_equal(g, o, "640x480 D=64 adaptive weights")
+    assert g[2].mean() > 0.5
+
+
+CROSS_1080 = {
+    "ad_census_cross": dict(cost1=1, cost2=3, aggr=3),
+    "census_cross": dict(cost1=3, cost2=0, aggr=3),
+    "rank_census_cross": dict(cost1=2, cost2=3, aggr=3, rank_rad=3),
+    "log_census_cross": dict(cost1=4, cost2=3, aggr=3),
+    "ad_census_box9x9": dict(cost1=1, cost2=3, aggr=1, box_rad=4),
+    "ncc7x7_box9x9": dict(cost1=5, cost2=0, aggr=1, box_rad=4, ncc_hrad=3, ncc_wrad=3),
+}
+
+
+@pytest.mark.parametrize("name", sorted(CROSS_1080))
+def test_config2_1920x1080(ctx, oracle_mod, name):
+    import rtstereo_gb300 as R
+    O = oracle_mod
+    kw = CROSS_1080[name]
+    L, Rr = pair(C2)
+    Lc, Rc = O.gray_to_rgb(L), O.gray_to_rgb(Rr)
+    p = R.params(disp_range=C2["D"], **kw)
+    # the benchmark's inputs: gray images only for the cross-based runs
+    g = ctx.pipeline(p, L, Rr) if kw["aggr"] == 3 else ctx.pipeline(p, L, Rr, Lc, Rc)
+    o = O.pipeline(oracle_params(O, p), L, Rr, Lc, Rc)
+    if kw["cost1"] == 4:
+        # CombineCost of the non-integer LoG differences takes the device expf, so
+        # near-ties may flip; every other cost is integer-valued and bit-exact
+        for a, b in zip(g[:3], o[:3]):
+            assert (a == b).mean() > 0.99
+    else:
+        assert_pair_equal(g, o, name)
+    assert g[2].mean() > 0.5
+
+
+def test_config2_adaptive_weights_1920x1080_rows(ctx, oracle_mod):
+    import rtstereo_gb300 as R
+    O = oracle_mod
+    L, Rr = pair(C2)
+    Lc, Rc = R.gray_to_rgb(L), R.gray_to_rgb(Rr)
+    Ll, Rl = R.rgb_to_lab(Lc), R.rgb_to_lab(Rc)
+    p = R.params(cost1=1, cost2=3, aggr=2, disp_range=C2["D"], right_view=0)
+    dl, _, _, cost = ctx.pipeline(p, L, Rr, Lc, Rc, Ll, Rl, want_cost=True)
+    op = oracle_params(O, p)
+    H = C2["H"]
+    # rows at both edges (windows cut by the image border) and inside
+    rows = [0, 7, 16, H // 3, H // 2 + 1, H - 17, H - 1]
+    vol = O.view_cost(op, L, Rr, Lc, Rc)
+    want = O.aw_l2r_rows(Ll, Rl, vol, rows, p.aw_rad, p.aw_gamma_s, p.aw_gamma_p)
+    for i, y in enumerate(rows):
+        assert bits_equal(cost[y], want[i]), f"row {y}: {(cost[y] != want[i]).sum()} costs differ"
+    # the fused arg-min (with the winner carry) over the whole returned volume
+    assert bits_equal(dl, O.wta(cost))
+
+
+def test_config3_batch_of_64_mixed_pairs(ctx, oracle_mod):
+    """One batch of the mixed workload (sizes 320x240 .. 1920x1080, D 32/64/128,
+    pair i made from seed 0xC3000 + i) through rts_batch_run, each pair against
+    the oracle."""
+    import torch
+
+    import rtstereo_gb300 as R
+    O = oracle_mod
+    sizes = [(320, 240), (640, 480), (1024, 768), (1280, 720), (1920, 1080)]
+    disps = [32, 64, 128]
+    rng = np.random.default_rng(0xC3000)
+    data = []
+    for i in range(64):
+        W, H = sizes[rng.integers(len(sizes))]
+        D = disps[rng.integers(len(disps))]
+        L, Rr, _ = R.synth_pair(0xC3000 + i, W, H, D, 6, 0, 2.0, 4)
+        data.append((L, Rr, D))
+    keep, pairs, params, outs = [], [], [], []
+    for L, Rr, D in data:
+        H, W = L.shape
+        dL, dR = torch.from_numpy(L).cuda(), torch.from_numpy(Rr).cuda()
+        o = [torch.zeros((H, W), dtype=torch.uint8, device="cuda") for _ in range(3)]
+        keep.append((dL, dR, o))
+        pairs.append(R.Pair(W, H, dL.data_ptr(), dR.data_ptr(), None, None, None, None))
+        params.append(R.params(disp_range=D))
+        outs.append(R.Out(o[0].data_ptr(), o[1].data_ptr(), o[2].data_ptr(), None))
+    ctx.batch_run(pairs, params, outs)
+    torch.cuda.synchronize()
+    for i, ((L, Rr, D), (_, _, o)) in enumerate(zip(data, keep)):
+        g = [t.cpu().numpy() for t in o]
+        want = O.pipeline(O.params(D=D), L, Rr, O.gray_to_rgb(L), O.gray_to_rgb(Rr))
+        assert_pair_equal(g, want, f"pair {i} ({L.shape[1]}x{L.shape[0]}, D={D})")
+
+
+@pytest.mark.parametrize("which", ["c1_aw_640x480", "c2_cross_1920x1080", "c2_aw_1920x1080"])
+def test_fp16_form_agreement(ctx, which):
+    """FP16 storage with fp32 accumulation: at least 99.5 % of the disparities
+    of both views and of the mask equal the plain form's (which is bit-exact to
+    the oracle) on the benchmark pairs."""
+    import rtstereo_gb300 as R
+    cfg, kw = {"c1_aw_640x480": (C1, dict(aggr=2)), "c2_cross_1920x1080": (C2, dict(aggr=3)),
+               "c2_aw_1920x1080": (C2, dict(aggr=2))}[which]
+    L, Rr = pair(cfg)
+    Lc, Rc = R.gray_to_rgb(L), R.gray_to_rgb(Rr)
+    Ll, Rl = R.rgb_to_lab(Lc), R.rgb_to_lab(Rc)
+    args = (L, Rr) if kw["aggr"] == 3 else (L, Rr, Lc, Rc, Ll, Rl)
+    a = ctx.pipeline(R.params(disp_range=cfg["D"], precision=R.PREC_F32, **kw), *args)
+    b = ctx.pipeline(R.params(disp_range=cfg["D"], precision=R.PREC_F16, **kw), *args)
+    for name, x, y in zip(("left", "right", "mask"), a[:3], b[:3]):
+        agree = (x == y).mean()
+        print(f"{which} {name}: {100 * agree:.4f} % equal")
+        assert agree >= 0.995, (name, agree)
