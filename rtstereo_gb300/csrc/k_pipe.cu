@@ -393,8 +393,16 @@ __global__ void __launch_bounds__(kAwThreads, 2) k_aw_wta_pipe(const CT *__restr
                                                           const uint32_t *__restrict__ labt,
                                                           const float *__restrict__ pw, const float *__restrict__ G,
                                                           uint16_t *__restrict__ raw, int *__restrict__ row_last,
-                                                          float *__restrict__ cost_out, int H, int W, int D, int e) {
+                                                          float *__restrict__ cost_out, int H, int W, int D, int e,
+                                                          float zero) {
     const int r = e >> 1;
+    // zero: +0.0f from the host.  A packed multiply whose result feeds a packed add is
+    // contracted into one fused multiply-add by the compiler, even written as
+    // mul.rn / __fmul2_rn; a fused multiply-add with this zero as its addend (which
+    // the compiler cannot know is zero) rounds like the multiply alone and is not
+    // fused further, so the plain form's products C*w stay IEEE products, two to an
+    // instruction.
+    const float2 z2 = make_float2(zero, zero);
     constexpr int NT = kAwTX + kAwDC - 1;  // target columns of a tile
     constexpr int NTP = NT + 1;
     // cost rows: kAwCPitch floats, or kAwHPitch halves (16-byte rows for the copies)
@@ -410,8 +418,14 @@ __global__ void __launch_bounds__(kAwThreads, 2) k_aw_wta_pipe(const CT *__restr
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     constexpr int NW = kAwThreads / 32;
-    const int td = lane & 15;
-    const int px0 = 8 * warp + 4 * (lane >> 4);
+    // tap tile: warp (wx, wd) = (warp & 3, warp >> 2) takes pixels 16 wx .. 16 wx + 15 and
+    // disparities 32 wd .. 32 wd + 31 of the tile; lane (pg, dg) = (lane >> 3, lane & 7)
+    // four pixels px0 .. px0+3 and four disparities dd0 .. dd0+3 of those.  Per tap a
+    // warp reads 4 distinct reference weights, 11 distinct 16-byte target-weight
+    // runs and one new cost column of 32 x 4 values (the other three of a thread's
+    // window are in registers from the previous taps).
+    const int px0 = 16 * (warp & 3) + 4 * (lane >> 3);
+    const int dd0 = 32 * (warp >> 2) + 4 * (lane & 7);
     const int y = blockIdx.y, x0 = blockIdx.x * kAwTX;
     if (tid < kAwTX) {
         best_v[tid] = __int_as_float(0x7f800000);
@@ -420,11 +434,13 @@ __global__ void __launch_bounds__(kAwThreads, 2) k_aw_wta_pipe(const CT *__restr
     const bool vec = (D & 3) == 0;
 
     for (int dc0 = 0; dc0 < D; dc0 += kAwDC) {
-        unsigned long long sw[4][2], sc[4][2];
+        // sums of disparity pairs (dd0 + 2h, dd0 + 2h + 1) of pixel px0 + j, as float2 for
+        // the packed adds (each half an IEEE round-to-nearest operation)
+        float2 sw[4][2], sc[4][2];
 #pragma unroll
         for (int j = 0; j < 4; j++)
 #pragma unroll
-            for (int h = 0; h < 2; h++) sw[j][h] = sc[j][h] = 0ull;
+            for (int h = 0; h < 2; h++) sw[j][h] = sc[j][h] = make_float2(0.f, 0.f);
         const int tbase = x0 - dc0 - (kAwDC - 1);
         uint32_t cR[2], cT[4];
 #pragma unroll
@@ -564,10 +580,12 @@ __global__ void __launch_bounds__(kAwThreads, 2) k_aw_wta_pipe(const CT *__restr
             const float *Cs = asm_ + b * CS, *wRs = wR0 + b * e * kAwTX, *wTs = wT0 + b * e * NTP;
             float *wRn = wR0 + (b ^ 1) * e * kAwTX, *wTn = wT0 + (b ^ 1) * e * NTP;
 
-            const int ubase = px0 - 4 * td + kAwDC - 4;
-            const CT *cp = reinterpret_cast<const CT *>(Cs) + px0 * CP + 4 * td;
+            // target weights of entry (j, i): u = px0 + j - (dd0 + i) + 63, so a thread's
+            // seven are ub .. ub+6 (the eighth loaded is ub+7 <= 127, inside the row)
+            const int ub = px0 - dd0 + kAwDC - 4;
+            const CT *cp = reinterpret_cast<const CT *>(Cs) + px0 * CP + dd0;  // staged column px0 + kx
             const float *wrp = wRs + px0;
-            const float *wtp = wTs + ubase;
+            const float *wtp = wTs + ub;
             // four disparities of a staged cost column as floats
             auto col4 = [&](const CT *q, float *o) {
                 if constexpr (sizeof(CT) == 4) {
@@ -580,47 +598,78 @@ __global__ void __launch_bounds__(kAwThreads, 2) k_aw_wta_pipe(const CT *__restr
                     o[0] = f0.x; o[1] = f0.y; o[2] = f1.x; o[3] = f1.y;
                 }
             };
-            auto tap = [&](const float (*cw)[4], int cofs, const float *wr4, const float *wt7) {
-                float wr[4], wt[7];
+            // one tap over the thread's 4 pixels x 4 disparities; cw[j] is the cost column
+            // of pixel j at this tap.  Plain form (EXACT): w = wR*wT, sw += w, sc += C*w, each
+            // an IEEE operation (seq/AdaptiveWeightAggregation.cpp:100-103): w by scalar
+            // multiplies, C*w by the packed multiply-add with the opaque zero, the sums by
+            // packed adds.  FP16 form: sc = fma(C, w, sc).
+            auto tap = [&](const float (&cw)[4][4], const float *wr4, const float *wt8) {
+                float wr[4], wt[8];
                 const float4 a0 = *reinterpret_cast<const float4 *>(wr4);
                 wr[0] = a0.x; wr[1] = a0.y; wr[2] = a0.z; wr[3] = a0.w;
-                const float4 b0 = *reinterpret_cast<const float4 *>(wt7);
-                const float4 b1 = *reinterpret_cast<const float4 *>(wt7 + 4);
+                const float4 b0 = *reinterpret_cast<const float4 *>(wt8);
+                const float4 b1 = *reinterpret_cast<const float4 *>(wt8 + 4);
                 wt[0] = b0.x; wt[1] = b0.y; wt[2] = b0.z; wt[3] = b0.w;
-                wt[4] = b1.x; wt[5] = b1.y; wt[6] = b1.z;
+                wt[4] = b1.x; wt[5] = b1.y; wt[6] = b1.z; wt[7] = b1.w;
 #pragma unroll
                 for (int j = 0; j < 4; j++)
 #pragma unroll
                     for (int h = 0; h < 2; h++) {
-                        const unsigned long long w = pack2(__fmul_rn(wr[j], wt[j - 2 * h + 3]),
-                                                           __fmul_rn(wr[j], wt[j - 2 * h + 2]));
-                        const unsigned long long c = pack2(cw[j + cofs][2 * h], cw[j + cofs][2 * h + 1]);
-                        sw[j][h] = add2(sw[j][h], w);
-                        if constexpr (EXACT) sc[j][h] = add2(sc[j][h], mul2(c, w));
-                        else sc[j][h] = fma2(c, w, sc[j][h]);
+                        const float w0 = __fmul_rn(wr[j], wt[j - 2 * h + 3]);
+                        const float w1 = __fmul_rn(wr[j], wt[j - 2 * h + 2]);
+                        sw[j][h] = __fadd2_rn(sw[j][h], make_float2(w0, w1));
+                        if constexpr (EXACT)
+                            sc[j][h] = __fadd2_rn(sc[j][h], __ffma2_rn(make_float2(cw[j][2 * h], cw[j][2 * h + 1]),
+                                                                       make_float2(w0, w1), z2));
+                        else
+                            sc[j][h] = __ffma2_rn(make_float2(cw[j][2 * h], cw[j][2 * h + 1]), make_float2(w0, w1),
+                                                  sc[j][h]);
                     }
             };
+            // the cost window slides one column per tap: win holds columns kx .. kx+2 of
+            // the thread's first pixel, each tap adds column kx+3
+            float win[3][4];
+#pragma unroll
+            for (int q = 0; q < 3; q++) col4(cp + q * CP, win[q]);
             int kx = 0, sj = 0;
 #pragma unroll 1
-            for (; kx + 4 <= e; kx += 4, cp += 4 * CP, wrp += 4 * kAwTX, wtp += 4 * NTP, sj++) {
+            for (; kx + 4 <= e; kx += 4, sj++) {
                 // a slice of the next tap row's weights around this group of taps
                 const int ks = warp + NW * sj;
                 const bool dos = next && ks < e;
                 Slice sl;
                 if (dos) slice_issue(sl, ky + 1, ks, lnext);
-                float cw[7][4];
+                float nc[4][4];
 #pragma unroll
-                for (int q = 0; q < 7; q++) col4(cp + q * CP, cw[q]);
+                for (int u = 0; u < 4; u++) col4(cp + (kx + 3 + u) * CP, nc[u]);
 #pragma unroll
-                for (int u = 0; u < 4; u++) tap(cw, u, wrp + u * kAwTX, wtp + u * NTP);
+                for (int u = 0; u < 4; u++) {
+                    float cw[4][4];
+#pragma unroll
+                    for (int j = 0; j < 4; j++)
+#pragma unroll
+                        for (int i = 0; i < 4; i++) cw[j][i] = (u + j < 3) ? win[u + j][i] : nc[u + j - 3][i];
+                    tap(cw, wrp + (kx + u) * kAwTX, wtp + (kx + u) * NTP);
+                }
+#pragma unroll
+                for (int q = 0; q < 3; q++)
+#pragma unroll
+                    for (int i = 0; i < 4; i++) win[q][i] = nc[q + 1][i];
                 if (dos) slice_finish(sl, ky + 1, ks, wRn, wTn);
             }
 #pragma unroll 1
-            for (; kx < e; kx++, cp += CP, wrp += kAwTX, wtp += NTP) {
+            for (; kx < e; kx++) {
                 float cw[4][4];
+                col4(cp + (kx + 3) * CP, cw[3]);
 #pragma unroll
-                for (int q = 0; q < 4; q++) col4(cp + q * CP, cw[q]);
-                tap(cw, 0, wrp, wtp);
+                for (int q = 0; q < 3; q++)
+#pragma unroll
+                    for (int i = 0; i < 4; i++) cw[q][i] = win[q][i];
+                tap(cw, wrp + kx * kAwTX, wtp + kx * NTP);
+#pragma unroll
+                for (int q = 0; q < 3; q++)
+#pragma unroll
+                    for (int i = 0; i < 4; i++) win[q][i] = cw[q + 1][i];
             }
             // slices the groups did not reach (short windows)
             if (next)
@@ -638,9 +687,10 @@ __global__ void __launch_bounds__(kAwThreads, 2) k_aw_wta_pipe(const CT *__restr
         for (int j = 0; j < 4; j++)
 #pragma unroll
             for (int i = 0; i < 4; i++) {
-                const float v = __fdiv_rn(half2_of(sc[j][i >> 1], i & 1), half2_of(sw[j][i >> 1], i & 1));
-                outs[(px0 + j) * (kAwDC + 1) + 4 * td + i] = v;
-                const int x = x0 + px0 + j, dg = dc0 + 4 * td + i;
+                const float2 a2 = sc[j][i >> 1], b2 = sw[j][i >> 1];
+                const float v = __fdiv_rn((i & 1) ? a2.y : a2.x, (i & 1) ? b2.y : b2.x);
+                outs[(px0 + j) * (kAwDC + 1) + dd0 + i] = v;
+                const int x = x0 + px0 + j, dg = dc0 + dd0 + i;
                 if (cost_out && x < W && dg < D) cost_out[((size_t)y * W + x) * D + dg] = v;
             }
         __syncthreads();
@@ -780,12 +830,12 @@ rts_status aw_fused(rts_ctx *c, const rts_params &p, int H, int W, const void *v
         const size_t psmem = pipe_smem((size_t)kAwHPitch * 2);
         RTS_TRY(set_smem(c, k_aw_wta_pipe<__half, false>, psmem, "aw_wta_pipe"));
         k_aw_wta_pipe<__half, false><<<grid, kAwThreads, psmem, c->stream>>>((const __half *)vol, plr, plt, pw, g, raw,
-                                                                             rl, cost_out, H, W, p.disp_range, e);
+                                                                             rl, cost_out, H, W, p.disp_range, e, 0.f);
     } else {
         const size_t psmem = pipe_smem((size_t)kAwCPitch * 4);
         RTS_TRY(set_smem(c, k_aw_wta_pipe<float, true>, psmem, "aw_wta_pipe"));
         k_aw_wta_pipe<float, true><<<grid, kAwThreads, psmem, c->stream>>>((const float *)vol, plr, plt, pw, g, raw,
-                                                                           rl, cost_out, H, W, p.disp_range, e);
+                                                                           rl, cost_out, H, W, p.disp_range, e, 0.f);
     }
     count_launch(c);
     return check_launch(c, "aw_wta");
