@@ -114,6 +114,22 @@ def test_adaptive_weight_pipeline(ctx, oracle_mod, W, H, D, rad):
     assert_same(g, o)
 
 
+@pytest.mark.parametrize("prec", [0, 1])
+def test_cross_views_longest_arm_wide_disparity(ctx, oracle_mod, prec):
+    """The fused cross-based views at the longest arm they take (23: the largest
+    vertical ring, 72 rows, and eight 32-disparity chunks per lane for D = 200),
+    against the oracle; the FP16 form against the plain one."""
+    import rtstereo_gb300 as R
+    L, Rr = synth(0x23, 224, 40, 200, 4, 1)
+    if prec == 0:
+        g, o = run_both(ctx, oracle_mod, L, Rr, disp_range=200, aggr=3, cross_arm=23)
+        assert_same(g, o)
+    else:
+        a = ctx.pipeline(R.params(disp_range=200, aggr=3, cross_arm=23), L, Rr)
+        b = ctx.pipeline(R.params(disp_range=200, aggr=3, cross_arm=23, precision=R.PREC_F16), L, Rr)
+        assert (a[0] == b[0]).mean() > 0.99
+
+
 def test_fused_paths_match_oracle(ctx, oracle_mod):
     # no cost output requested: the fused kernels run where they exist
     for kw in (dict(disp_range=16, aggr=3), dict(disp_range=64, aggr=3), dict(disp_range=32, aggr=2, aw_rad=7),
