@@ -36,9 +36,14 @@ def test_roofline_fields():
     r = bench.roofline({"aw_wta": (2, 8.0)}, "aw_640x480_d64", 640, 480, 64, 2, peaks, "measured", p)
     assert r["bound"] == "fp32" and r["kernel"] == "k_aw_wta_pipe"
     assert r["ms_per_launch"] == pytest.approx(4.0)
-    assert r["flop_per_launch"] == pytest.approx(4 * 33 * 33 * 640 * 480 * 64)
+    assert r["ops_per_launch"] == pytest.approx(4 * 33 * 33 * 640 * 480 * 64)
     assert r["peak"] == pytest.approx(152 * 128 * 2000e6 / 1e12)
     assert r["frac"] == pytest.approx(r["achieved"] / r["peak"])
+    # the SM count is the device's (passed in), the FP16 form counts 3 operations a tap
+    r16 = bench.roofline({"aw_wta": (2, 8.0)}, "aw_640x480_d64", 640, 480, 64, 2, peaks, "measured",
+                         R.params(aggr=2, disp_range=64, precision=R.PREC_F16), sms=160)
+    assert r16["peak"] == pytest.approx(160 * 128 * 2000e6 / 1e12) and "160 SMs" in r16["peak_source"]
+    assert r16["ops_per_launch"] == pytest.approx(3 * 33 * 33 * 640 * 480 * 64)
     # cross-based: HBM stage model, 2 views x 2 crossings x S bytes per entry
     p = R.params(disp_range=128)
     stages = {"cross_hseg": (1, 1.0), "cross_vert_wta": (1, 2.0)}
@@ -69,6 +74,23 @@ def test_reference_arm_line():
     assert line["cpu_baseline"]["kind"] == ("reference" if oracle.have_reference() else "port")
     assert line["cpu_baseline"]["cores"] >= 1 and line["cpu_baseline"]["value"] == line["value"]
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["d2h_bytes_per_step"] == 0
+    # the same config object as the GPU arm prints for this workload
+    import bench as B
+    assert line["config"] == B.workload_config("cross_384x288_d16", "f32", 1)
+
+
+def test_reference_arm_does_not_load_the_library():
+    """The CPU reference arm makes its inputs with the oracle's copy of the
+    generator: neither it nor its workers map the product library."""
+    import subprocess
+    code = ("import sys; sys.argv = ['bench.py', '--impl', 'reference', '--steps', '1', '--warmup', '0', "
+            "'--cpu-rows', '4', '--workload', 'cross_384x288_d16']\n"
+            "if __name__ == '__main__':\n"
+            "    import bench; bench.main()\n"
+            "    print('MAPS', 'librtstereo_gb300' in open('/proc/self/maps').read())\n")
+    out = subprocess.run([sys.executable, "-c", code], cwd=ROOT, capture_output=True, text=True, timeout=600)
+    assert out.returncode == 0, out.stderr[-2000:]
+    assert "MAPS False" in out.stdout
 
 
 def test_latency_target_record():
