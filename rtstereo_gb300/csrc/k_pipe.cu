@@ -387,14 +387,17 @@ __global__ void __launch_bounds__(kAwThreads, 3) k_aw_wta(const CT *__restrict__
 // ky + 2 are staged; one barrier per tap row.  The arithmetic per entry is
 // k_aw_wta's: EXACT (plain form, f32 volume) the reference's order, unfused;
 // otherwise (FP16 form, f16 volume staged as f16, D a multiple of 8) one FMA.
-template <typename CT, bool EXACT>
+// E: the window edge as a constant (33, the reference driver's 33 x 33 window), so
+// that the tap loop unrolls whole, or 0 for the edge of the e argument.
+template <typename CT, bool EXACT, int E>
 __global__ void __launch_bounds__(kAwThreads, 2) k_aw_wta_pipe(const CT *__restrict__ vol,
                                                           const uint32_t *__restrict__ labr,
                                                           const uint32_t *__restrict__ labt,
                                                           const float *__restrict__ pw, const float *__restrict__ G,
                                                           uint16_t *__restrict__ raw, int *__restrict__ row_last,
-                                                          float *__restrict__ cost_out, int H, int W, int D, int e,
+                                                          float *__restrict__ cost_out, int H, int W, int D, int e_arg,
                                                           float zero) {
+    const int e = E ? E : e_arg;
     const int r = e >> 1;
     // zero: +0.0f from the host.  A packed multiply whose result feeds a packed add is
     // contracted into one fused multiply-add by the compiler, even written as
@@ -632,7 +635,7 @@ __global__ void __launch_bounds__(kAwThreads, 2) k_aw_wta_pipe(const CT *__restr
 #pragma unroll
             for (int q = 0; q < 3; q++) col4(cp + q * CP, win[q]);
             int kx = 0, sj = 0;
-#pragma unroll 1
+#pragma unroll(E ? 8 : 1)
             for (; kx + 4 <= e; kx += 4, sj++) {
                 // a slice of the next tap row's weights around this group of taps
                 const int ks = warp + NW * sj;
@@ -657,7 +660,7 @@ __global__ void __launch_bounds__(kAwThreads, 2) k_aw_wta_pipe(const CT *__restr
                     for (int i = 0; i < 4; i++) win[q][i] = nc[q + 1][i];
                 if (dos) slice_finish(sl, ky + 1, ks, wRn, wTn);
             }
-#pragma unroll 1
+#pragma unroll(E ? 3 : 1)
             for (; kx < e; kx++) {
                 float cw[4][4];
                 col4(cp + (kx + 3) * CP, cw[3]);
@@ -828,14 +831,16 @@ rts_status aw_fused(rts_ctx *c, const rts_params &p, int H, int W, const void *v
         RTS_TRY(go(k_aw_wta<__half, false>, (const __half *)vol));
     } else if (half) {
         const size_t psmem = pipe_smem((size_t)kAwHPitch * 2);
-        RTS_TRY(set_smem(c, k_aw_wta_pipe<__half, false>, psmem, "aw_wta_pipe"));
-        k_aw_wta_pipe<__half, false><<<grid, kAwThreads, psmem, c->stream>>>((const __half *)vol, plr, plt, pw, g, raw,
-                                                                             rl, cost_out, H, W, p.disp_range, e, 0.f);
+        auto kern = e == 33 ? k_aw_wta_pipe<__half, false, 33> : k_aw_wta_pipe<__half, false, 0>;
+        RTS_TRY(set_smem(c, kern, psmem, "aw_wta_pipe"));
+        kern<<<grid, kAwThreads, psmem, c->stream>>>((const __half *)vol, plr, plt, pw, g, raw, rl, cost_out, H, W,
+                                                     p.disp_range, e, 0.f);
     } else {
         const size_t psmem = pipe_smem((size_t)kAwCPitch * 4);
-        RTS_TRY(set_smem(c, k_aw_wta_pipe<float, true>, psmem, "aw_wta_pipe"));
-        k_aw_wta_pipe<float, true><<<grid, kAwThreads, psmem, c->stream>>>((const float *)vol, plr, plt, pw, g, raw,
-                                                                           rl, cost_out, H, W, p.disp_range, e, 0.f);
+        auto kern = e == 33 ? k_aw_wta_pipe<float, true, 33> : k_aw_wta_pipe<float, true, 0>;
+        RTS_TRY(set_smem(c, kern, psmem, "aw_wta_pipe"));
+        kern<<<grid, kAwThreads, psmem, c->stream>>>((const float *)vol, plr, plt, pw, g, raw, rl, cost_out, H, W,
+                                                     p.disp_range, e, 0.f);
     }
     count_launch(c);
     return check_launch(c, "aw_wta");
