@@ -521,26 +521,39 @@ __global__ void __launch_bounds__(kAwThreads, 2) k_aw_wta_pipe(const CT *__restr
             bool ok[6];
             float g[6];
         };
+        // (every caller passes k < e, so the reference index lane + 32 m + k <= 63 + 2r
+        // stays inside its row, and the target index u + k only passes the row's end
+        // for u = 127, the padding target of lane 31)
         auto slice_issue = [&](Slice &sl, int ky, int k, int slot) {
             const uint32_t *LR = labbase + slot * (LRN + LTN), *LT = LR + LRN;
-            const size_t crow = (size_t)(y + ky) * W;
 #pragma unroll
             for (int m = 0; m < 2; m++) {
-                const uint32_t q = LR[imin(lane + 32 * m + k, LRN - 1)];
-                sl.ok[m] = k < e && !((q | cR[m]) & kLabOut);
+                const uint32_t q = LR[lane + 32 * m + k];
+                sl.ok[m] = !((q | cR[m]) & kLabOut);
                 const uint32_t ad = __vabsdiffu4(cR[m], q);
                 sl.idx[m] = __dp4a(ad, ad, 0u);
             }
+            uint32_t qt[4];
+#pragma unroll
+            for (int m = 0; m < 3; m++) qt[m] = LT[lane + 32 * m + k];
+            qt[3] = LT[imin(lane + 96 + k, LTN - 1)];
+            if (wrapped_tile) {
+                // targets that wrapped around the left edge: their taps come from the
+                // other end of the row (block-uniform branch)
+                const size_t crow = (size_t)(y + ky) * W;
+#pragma unroll
+                for (int m = 0; m < 4; m++) {
+                    const int u = lane + 32 * m;
+                    if (tbase + u < 0) {
+                        const int xc = tbase + u + W + k - r;
+                        qt[m] = (xc >= 0 && xc < W) ? labt[crow + xc] : kLabOut;
+                    }
+                }
+            }
 #pragma unroll
             for (int m = 0; m < 4; m++) {
-                const int u = lane + 32 * m;
-                uint32_t q = LT[imin(u + k, LTN - 1)];
-                if (wrapped_tile && tbase + u < 0 && k < e) {
-                    const int xc = tbase + u + W + k - r;
-                    q = (xc >= 0 && xc < W) ? labt[crow + xc] : kLabOut;
-                }
-                sl.ok[2 + m] = k < e && u < NT && !((q | cT[m]) & kLabOut);
-                const uint32_t ad = __vabsdiffu4(cT[m], q);
+                sl.ok[2 + m] = (m < 3 || lane < 31) && !((qt[m] | cT[m]) & kLabOut);
+                const uint32_t ad = __vabsdiffu4(cT[m], qt[m]);
                 sl.idx[2 + m] = __dp4a(ad, ad, 0u);
             }
 #pragma unroll
