@@ -732,6 +732,69 @@ def f16_record(bench, plain):
     return rec
 
 
+def run_modules(args, rank, world):
+    """The drop-in module path: the reference driver's left-view chain for
+    AD + census, cross-based aggregation (seq/Main.cpp:180-257) called module by
+    module through the seq-signature entry points with HOST buffers, as a caller
+    of include/rts_seq_compat.hpp does (every call copies its inputs to the device
+    and its outputs back, and synchronises).  Beside it the fused pipeline on the
+    same pair, left view only, with HOST buffers."""
+    import torch
+
+    import rtstereo_gb300 as R
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    name = args.workload
+    (W, H, D, c1, c2, ag, extra), (L, Rr, Lc, Rc, Ll, Rl) = make_inputs(name)
+    if (c1, c2, ag) != (1, 3, 3):
+        raise SystemExit("--module-path: an AD + census, cross-based workload")
+    ctx = R.Context(dev)
+
+    def chain(t):
+        def timed(key, fn):
+            t0 = time.perf_counter()
+            v = fn()
+            t[key] = t.get(key, 0.0) + (time.perf_counter() - t0) * 1e3
+            return v
+        ad = timed("pixelBasedCostL2R_Color", lambda: ctx.pixelBasedCostL2R_Color(Lc, Rc, D, trunc=24.0))
+        bl = timed("calcCensusTrans x2", lambda: ctx.calcCensusTrans(L))
+        br = timed("calcCensusTrans x2", lambda: ctx.calcCensusTrans(Rr))
+        hm = timed("calcHammingDist", lambda: ctx.calcHammingDist(bl, br, D))
+        cc = timed("combineCost", lambda: ctx.combineCost(ad, hm, 10.0, 10.0))
+        hl, vl = timed("findCross x2", lambda: ctx.findCross(Lc))
+        hr, vr = timed("findCross x2", lambda: ctx.findCross(Rc))
+        pre = timed("aggregate_cost_horizontal", lambda: ctx.aggregate_cost_horizontal(cc))
+        agg = timed("cross_stereo_aggregation", lambda: ctx.cross_stereo_aggregation(pre, hl, hr, vl, vr))
+        return timed("WTA", lambda: ctx.WTA(agg))
+
+    for _ in range(args.warmup):
+        chain({})
+    t = {}
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        d_mod = chain(t)
+    ms = (time.perf_counter() - t0) * 1e3 / args.steps
+    p = R.params(disp_range=D, right_view=0)
+    for _ in range(args.warmup):
+        ctx.pipeline(p, L, Rr)
+    t1 = time.perf_counter()
+    for _ in range(args.steps):
+        d_fused = ctx.pipeline(p, L, Rr)[0]
+    ms_fused = (time.perf_counter() - t1) * 1e3 / args.steps
+    if rank == 0:
+        print(json.dumps({
+            "metric": "MDE/s", "value": W * H * D / 1e6 / (ms / 1e3), "unit": "MDE/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic random-dot stereo pair (seeded, no dataset)",
+            "config": {"workload": name, "width": W, "height": H, "disp_range": D,
+                       "pipeline": "left view, AD(trunc 24)+census, cross-based, WTA; module by module, HOST buffers",
+                       "path": "seq-signature module entry points (rts_seq_compat.hpp), host wall clock"},
+            "modules_ms_per_step": {k: v / args.steps for k, v in t.items()},
+            "fused_left_view_ms": ms_fused, "fused_speedup": ms / ms_fused,
+            "same_disparities": bool(np.array_equal(d_mod, d_fused))}), flush=True)
+
+
 def run_ours(args, rank, world):
     import torch
     dev = int(os.environ.get("LOCAL_RANK", "0"))
@@ -855,6 +918,8 @@ def main():
     ap.add_argument("--cpu-rows", type=int, default=None,
                     help="rows per CPU strip (default 48 for the 1-thread baseline, 24 for --impl reference)")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--module-path", action="store_true",
+                    help="time the drop-in module path (seq-signature calls, HOST buffers) on the workload")
     ap.add_argument("--no-extra", action="store_true",
                     help="default workload: skip the f16 / c2_cross_1080p / serve sub-records")
     ap.add_argument("--serve-rate", type=float, default=600.0,
@@ -870,6 +935,8 @@ def main():
         run_batch(args, rank, world)
     elif args.workload == "serve_poisson":
         run_serve(args, rank, world)
+    elif args.module_path:
+        run_modules(args, rank, world)
     else:
         run_ours(args, rank, world)
 
