@@ -262,7 +262,7 @@ __global__ void __launch_bounds__(256) k_ncc_tiled(const uint8_t *__restrict__ r
         __syncthreads();
         // u index of (j, i): px0 + j - d0 - i + 63
         const int ub = px0 - d0 + kNccTD - 4;
-#pragma unroll 1
+#pragma unroll 7
         for (int k = 0; k < nk; k++) {
             unsigned long long r[4], tt[8];
             const ulonglong2 ra = *reinterpret_cast<const ulonglong2 *>(&rq[k][ncc_swz(px0)]);
