@@ -847,6 +847,8 @@ NCU_BYTES_PER_ENTRY = {("cross_vert_wta", 0): 4.16, ("cross_hseg", 0): 4.00,
 # ncu DRAM bytes of one plain-form adaptive-weight launch (k_aw_wta_pipe, one view)
 # at 640x480, D=64 (the full capture of that launch)
 NCU_AW_BYTES = {(640, 480, 64): 85.28e6}
+# DRAM bytes (read + write) of one k_box_best_dp launch, ncu at 1920x1080, D=128, r=4
+NCU_BOX_BYTES = {(1920, 1080, 128, 4): 1.1375e9}
 
 
 def roofline(stages, name, W, H, D, ag, peaks, src, p, ms_pair=None, sms=152):
@@ -876,6 +878,19 @@ def roofline(stages, name, W, H, D, ag, peaks, src, p, ms_pair=None, sms=152):
                 "peak_source": f"FP32 pipe: {sms} SMs (device attribute) x 128 lanes x {mhz:.0f} MHz "
                                f"({src} max clock), one operation per lane per clock; no tensor-core or HBM "
                                f"bound applies (DRAM < 1% busy)"}
+    if kname == "box_wta":
+        # one launch = one view: (2r+1)^2 sequential FP32 adds per entry (the
+        # reference's single chain), no other bound near (the volume read once)
+        ops = float((2 * p.box_rad + 1) ** 2 * E)
+        achieved = ops / (per_launch_ms / 1e3) / 1e12
+        mhz = peaks.get("sm_max_mhz", 2070.0)
+        peak = sms * 128 * mhz * 1e6 / 1e12
+        return {"bound": "fp32", "kernel": "k_box_best_dp" if (D % 2 == 0 and D > 32) else "k_box_best",
+                "achieved": achieved, "peak": peak, "unit": "T FP32-pipe op/s", "frac": achieved / peak,
+                "traffic": NCU_BOX_BYTES.get((W, H, D, p.box_rad)), "launches": launches,
+                "ms_per_launch": per_launch_ms, "ops_per_launch": ops,
+                "peak_source": f"FP32 pipe: {sms} SMs (device attribute) x 128 lanes x {mhz:.0f} MHz "
+                               f"({src} max clock), one operation per lane per clock"}
     # HBM stage model (one launch = both views): the cost volume crosses HBM four
     # times per view at S bytes an entry; the row-segment kernel owns the first two
     # crossings (written by matching and combining, read by aggregation), the

@@ -130,6 +130,127 @@ __global__ void __launch_bounds__(256) k_box_best(const float *__restrict__ vol,
     }
 }
 
+// The same box mean and arg-min with a lane on two adjacent disparities (even D):
+// block per (16 x 8 pixel tile, 64 disparities), the staged cells [TH][TW][64] so
+// that a lane's pair {d, d + 1} is one 8-byte shared load that feeds a packed add
+// directly (no register moves to pair pixels).  A warp takes one tile row, all 16
+// pixels at once; each sum is the reference's single chain as above.
+constexpr int kBoxDpTX = 16, kBoxDpTY = 8;
+
+// cp.async of one tile's cells into bt2 (every cell in flight at once)
+template <int R>
+__device__ __forceinline__ void box_dp_stage(float2 *bt2, const float *__restrict__ vol, int H, int W, int D, int x0,
+                                             int y0, int d) {
+    constexpr int TW = kBoxDpTX + 2 * R, TH = kBoxDpTY + 2 * R;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    // single wrap as in seq/ConstBlockAggregation.cpp:19-24; cells past the last
+    // pixel's window are clamped into range (never read); zero fill past D
+    const bool inner = x0 >= R && x0 + kBoxDpTX + R <= W;
+    const int dofs = d < D ? d : 0;
+    const unsigned nbytes = d < D ? 8u : 0u;
+    for (int i = warp; i < TH; i += 8) {
+        const int yy = wrap1(imin(y0 - R + i, H - 1 + R), H);
+        const float *rowp = vol + (size_t)yy * W * D + dofs;
+        unsigned dst = (unsigned)__cvta_generic_to_shared(bt2 + i * TW * 32 + lane);
+        if (inner) {
+            const float *src = rowp + (size_t)(x0 - R) * D;
+#pragma unroll 8
+            for (int j = 0; j < TW; j++, src += D, dst += 256)
+                asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(dst), "l"(src), "r"(nbytes)
+                             : "memory");
+        } else {
+            for (int j = 0; j < TW; j++, dst += 256) {
+                const int xx = wrap1(imin(x0 - R + j, W - 1 + R), W);
+                asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(dst),
+                             "l"(rowp + (size_t)xx * D), "r"(nbytes)
+                             : "memory");
+            }
+        }
+    }
+}
+
+// the sums, means and per-pixel minimum of one staged tile (warp = tile row)
+template <int R, int POS>
+__device__ __forceinline__ void box_dp_tile(const float2 *bt2, unsigned long long *__restrict__ best, int H, int W,
+                                            int D, int argmax, float rcp_area, int x0, int y0, int d) {
+    constexpr int TW = kBoxDpTX + 2 * R, AREA = (2 * R + 1) * (2 * R + 1);
+    constexpr int G = kBoxDpTX;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int y = y0 + warp;
+    if (y >= H) return;
+    float2 s[G];
+#pragma unroll
+    for (int m = 0; m < G; m++) s[m] = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int dy = 0; dy <= 2 * R; dy++) {
+        const float2 *rp = bt2 + (warp + dy) * TW * 32 + lane;
+        float2 v[TW];
+#pragma unroll
+        for (int k = 0; k < TW; k++) v[k] = rp[k * 32];
+#pragma unroll
+        for (int m = 0; m < G; m++)
+#pragma unroll
+            for (int dx = 0; dx <= 2 * R; dx++) s[m] = __fadd2_rn(s[m], v[m + dx]);
+    }
+    // The mean is sum / AREA correctly rounded (seq/ConstBlockAggregation.cpp:31):
+    // q0 = sum * y with y = RN(1 / AREA), the residual r = sum - AREA * q0 by FMA,
+    // q = RN(q0 + r * y) (Markstein's correction).  With |y - 1/AREA| <= 2^-24 / AREA
+    // relative, q0 is within 1.5 ulp of the quotient, so r is an integer multiple of
+    // ulp(q0) below 1.5 * AREA ulps: exact.  q0 + r * y then differs from the quotient
+    // by at most 1.5 * 2^-24 ulp, less than the quotient's least distance to a
+    // rounding midpoint (ulp / (2 * AREA): AREA is odd), so q is the correctly rounded
+    // quotient -- for sums of either sign whose quotient is normal.  Sums of
+    // non-negative costs are finite and >= +0, and their key is their bit pattern;
+    // other sums outside [2^-100, 2^126] in magnitude (zero, NaN, infinity) divide.
+    const uint32_t flip = argmax ? 0xffffffffu : 0u;
+    const float2 ry = make_float2(rcp_area, rcp_area), na = make_float2(-(float)AREA, -(float)AREA);
+#pragma unroll
+    for (int m = 0; m < G; m++) {
+        const int x = x0 + m;
+        uint32_t k0, k1;
+        if (POS) {
+            const float2 q0 = __fmul2_rn(s[m], ry);
+            const float2 q = __ffma2_rn(__ffma2_rn(na, q0, s[m]), ry, q0);
+            k0 = (__float_as_uint(q.x) | 0x80000000u) ^ flip;  // wta_key of a float >= +0
+            k1 = (__float_as_uint(q.y) | 0x80000000u) ^ flip;
+        } else {
+            float q[2];
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                const float sm = h ? s[m].y : s[m].x, a = fabsf(sm);
+                if (a >= 0x1p-100f && a <= 0x1p+126f) {
+                    const float q0 = __fmul_rn(sm, rcp_area);
+                    q[h] = __fmaf_rn(__fmaf_rn(-(float)AREA, q0, sm), rcp_area, q0);
+                } else {
+                    q[h] = __fdiv_rn(sm, (float)AREA);
+                }
+            }
+            k0 = wta_key(q[0], d, argmax);
+            k1 = wta_key(q[1], d + 1, argmax);
+        }
+        if (d >= D) k0 = k1 = 0xffffffffu;  // D even: d < D implies d + 1 < D
+        // the lane's winner, the lower disparity on a tie
+        const uint32_t key = k1 < k0 ? k1 : k0;
+        const uint32_t kd = k1 < k0 ? (uint32_t)(d + 1) : (uint32_t)d;
+        const uint32_t mn = __reduce_min_sync(0xffffffffu, key);
+        const uint32_t bd = __reduce_min_sync(0xffffffffu, key == mn ? kd : 0xffffffffu);
+        if (lane == 0 && x < W) atomicMin(best + (size_t)y * W + x, ((unsigned long long)mn << 32) | bd);
+    }
+}
+
+// one tile per block
+template <int R, int POS>
+__global__ void __launch_bounds__(256, 2) k_box_best_dp(const float *__restrict__ vol,
+                                                        unsigned long long *__restrict__ best, int H, int W, int D,
+                                                        int argmax, float rcp_area) {
+    extern __shared__ float2 bt2[];  // [TH][TW][32] pairs
+    const int x0 = blockIdx.x * kBoxDpTX, y0 = blockIdx.y * kBoxDpTY, d = blockIdx.z * 64 + 2 * (threadIdx.x & 31);
+    box_dp_stage<R>(bt2, vol, H, W, D, x0, y0, d);
+    asm volatile("cp.async.wait_all;\n" ::: "memory");
+    __syncthreads();
+    box_dp_tile<R, POS>(bt2, best, H, W, D, argmax, rcp_area, x0, y0, d);
+}
+
 // per-pixel minimum -> WTA winner word and row summary (see k_wta.cu)
 __global__ void k_best_raw(const unsigned long long *__restrict__ best, uint16_t *__restrict__ raw,
                            int *__restrict__ row_last, int H, int W) {
@@ -374,7 +495,10 @@ void launch_box(cudaStream_t s, const float *in, float *out, int H, int W, int D
 bool box_best_supported(int r) { return r >= 1 && r <= 8; }
 void launch_box_best(cudaStream_t s, const float *vol, unsigned long long *best, uint16_t *raw, int *row_last, int H,
                      int W, int D, int r, int argmax, int pos) {
-    const dim3 g((W + kBoxTX - 1) / kBoxTX, (H + kBoxTY - 1) / kBoxTY, (D + 31) / 32);
+    // disparity pairs for even D above one warp's 32; else a lane per disparity
+    const bool dp = D % 2 == 0 && D > 32;
+    const dim3 g = dp ? dim3((W + kBoxDpTX - 1) / kBoxDpTX, (H + kBoxDpTY - 1) / kBoxDpTY, (D + 63) / 64)
+                      : dim3((W + kBoxTX - 1) / kBoxTX, (H + kBoxTY - 1) / kBoxTY, (D + 31) / 32);
     const int area = (2 * r + 1) * (2 * r + 1);
     const float rcp_area = 1.0f / (float)area;  // host IEEE division: correctly rounded
     auto go = [&](auto kern, int R) {
@@ -382,10 +506,20 @@ void launch_box_best(cudaStream_t s, const float *vol, unsigned long long *best,
         cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         kern<<<g, 256, smem, s>>>(vol, best, H, W, D, argmax, rcp_area);
     };
-#define RTS_BOX(RR)                                \
-    case RR:                                       \
-        if (pos) go(k_box_best<RR, 1>, RR);        \
-        else go(k_box_best<RR, 0>, RR);            \
+    auto go_dp = [&](auto kern, int R) {
+        const size_t smem = (size_t)(kBoxDpTX + 2 * R) * (kBoxDpTY + 2 * R) * 64 * sizeof(float);
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        kern<<<g, 256, smem, s>>>(vol, best, H, W, D, argmax, rcp_area);
+    };
+#define RTS_BOX(RR)                                                \
+    case RR:                                                       \
+        if (dp) {                                                  \
+            if (pos) go_dp(k_box_best_dp<RR, 1>, RR);              \
+            else go_dp(k_box_best_dp<RR, 0>, RR);                  \
+        } else {                                                   \
+            if (pos) go(k_box_best<RR, 1>, RR);                    \
+            else go(k_box_best<RR, 0>, RR);                        \
+        }                                                          \
         break;
     switch (r) {
         RTS_BOX(1)

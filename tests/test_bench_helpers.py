@@ -44,6 +44,12 @@ def test_roofline_fields():
                          R.params(aggr=2, disp_range=64, precision=R.PREC_F16), sms=160)
     assert r16["peak"] == pytest.approx(160 * 128 * 2000e6 / 1e12) and "160 SMs" in r16["peak_source"]
     assert r16["ops_per_launch"] == pytest.approx(3 * 33 * 33 * 640 * 480 * 64)
+    # box: FP32-pipe bound, (2r+1)^2 adds per entry, one launch per view
+    p = R.params(aggr=1, disp_range=128, box_rad=4)
+    r = bench.roofline({"box_wta": (2, 2.0), "left_view": (1, 1.5)}, "box_1920x1080_d128", 1920, 1080, 128, 1,
+                       peaks, "measured", p)
+    assert r["bound"] == "fp32" and r["kernel"] == "k_box_best_dp" and r["ms_per_launch"] == pytest.approx(1.0)
+    assert r["ops_per_launch"] == pytest.approx(81 * 1920 * 1080 * 128) and r["traffic"] == pytest.approx(1.1375e9)
     # cross-based: HBM stage model, 2 views x 2 crossings x S bytes per entry
     p = R.params(disp_range=128)
     stages = {"cross_hseg": (1, 1.0), "cross_vert_wta": (1, 2.0)}
