@@ -891,6 +891,21 @@ def roofline(stages, name, W, H, D, ag, peaks, src, p, ms_pair=None, sms=152):
                 "ms_per_launch": per_launch_ms, "ops_per_launch": ops,
                 "peak_source": f"FP32 pipe: {sms} SMs (device attribute) x 128 lanes x {mhz:.0f} MHz "
                                f"({src} max clock), one operation per lane per clock"}
+    if kname == "cost" and p.cost1 == 5 and p.cost2 == 0:
+        # NCC volume, one stage per view (k_ncc_tiled after the window means): per
+        # tap per entry rv*tv, (rv*rv)*tv, ((rv*rv)*tv)*tv and the two sums -- rv,
+        # rv*rv and tv are per pixel and tap, shared by every disparity
+        taps = (2 * p.ncc_hrad + 1) * (2 * p.ncc_wrad + 1)
+        ops = float(5 * taps * E)
+        achieved = ops / (per_launch_ms / 1e3) / 1e12
+        mhz = peaks.get("sm_max_mhz", 2070.0)
+        peak = sms * 128 * mhz * 1e6 / 1e12
+        return {"bound": "fp32", "kernel": "k_ncc_tiled", "achieved": achieved, "peak": peak,
+                "unit": "T FP32-pipe op/s", "frac": achieved / peak, "traffic": None, "launches": launches,
+                "ms_per_launch": per_launch_ms, "ops_per_launch": ops, "ops_per_tap": 5,
+                "peak_source": f"FP32 pipe: {sms} SMs (device attribute) x 128 lanes x {mhz:.0f} MHz "
+                               f"({src} max clock), one operation per lane per clock; the stage also holds "
+                               f"the window means (2-3 % of it)"}
     # HBM stage model (one launch = both views): the cost volume crosses HBM four
     # times per view at S bytes an entry; the row-segment kernel owns the first two
     # crossings (written by matching and combining, read by aggregation), the

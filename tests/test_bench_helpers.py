@@ -50,6 +50,12 @@ def test_roofline_fields():
                        peaks, "measured", p)
     assert r["bound"] == "fp32" and r["kernel"] == "k_box_best_dp" and r["ms_per_launch"] == pytest.approx(1.0)
     assert r["ops_per_launch"] == pytest.approx(81 * 1920 * 1080 * 128) and r["traffic"] == pytest.approx(1.1375e9)
+    # NCC 7x7 volume: FP32-pipe bound, 5 operations per tap per entry
+    p = R.params(aggr=1, disp_range=128, box_rad=4, cost1=5, cost2=0, ncc_hrad=3, ncc_wrad=3)
+    r = bench.roofline({"cost": (2, 6.0), "box_wta": (2, 2.0)}, "ncc_box_1920x1080_d128", 1920, 1080, 128, 1,
+                       peaks, "measured", p)
+    assert r["bound"] == "fp32" and r["kernel"] == "k_ncc_tiled" and r["ms_per_launch"] == pytest.approx(3.0)
+    assert r["ops_per_launch"] == pytest.approx(5 * 49 * 1920 * 1080 * 128)
     # cross-based: HBM stage model, 2 views x 2 crossings x S bytes per entry
     p = R.params(disp_range=128)
     stages = {"cross_hseg": (1, 1.0), "cross_vert_wta": (1, 2.0)}
