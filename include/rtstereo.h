@@ -198,7 +198,9 @@ typedef struct rts_params {
     int cross_tau;    /* seq/CrossBasedAggregation.h:9: 20 */
     float ad_trunc;   /* seq/Main.cpp:128: 24 (AD first cost with cross-based aggregation) */
     int right_view;   /* 1: right view as flip(L2R(flip R, flip L)) and the cross-check mask */
-    int precision;    /* RTS_PREC_F32 (plain) or RTS_PREC_F16 (fp16 storage, fp32 accumulation) */
+    int precision;    /* RTS_PREC_F32 (plain) or RTS_PREC_F16 (fp16 storage, fp32 accumulation; with
+                         adaptive weights the right view is read from the left view's final volume,
+                         equal to the mirrored pipeline's up to the order of its sums) */
     int median_ksize; /* 0: off; odd 3..15 (cross-based only): the arms are found on median-filtered
                          copies of the colour images, the costs on the unfiltered ones, as the OpenCL
                          driver does (opencl/Main.cpp:342-343, medianBlur with 3) */

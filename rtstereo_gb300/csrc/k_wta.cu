@@ -11,6 +11,7 @@
 //      a ballot scan.
 // raw[p] = found ? 0x100 | winner : 0.  row_last must start at -1.
 #include "rts_common.cuh"
+#include "rts_diag.cuh"
 
 namespace rts {
 
@@ -69,6 +70,13 @@ __global__ void k_wta_fill(const uint16_t *__restrict__ raw, const int *__restri
     }
 }
 
+// The right view's winners from the left view's final volume (rts_diag.cuh):
+// block per (row, 256 right-image pixels).
+__global__ void __launch_bounds__(kDiagT) k_wta_diag(const float *__restrict__ vol, uint16_t *__restrict__ raw,
+                                                     int *__restrict__ row_last, int W, int D) {
+    wta_diag_item(vol, raw, row_last, W, D, blockIdx.y, blockIdx.x * kDiagT);
+}
+
 // seq/CrossCheck.cpp:10-23
 __global__ void k_cross_check(const uint8_t *__restrict__ dl, const uint8_t *__restrict__ dr,
                               uint8_t *__restrict__ mask, int H, int W) {
@@ -95,6 +103,9 @@ __global__ void k_flip(const uint8_t *__restrict__ in, uint8_t *__restrict__ out
 void launch_wta_local(cudaStream_t s, const float *cost, uint16_t *raw, int *row_last, int H, int W, int D,
                       int argmax) {
     k_wta_local<<<dim3((W + 127) / 128, H), 128, 0, s>>>(cost, raw, row_last, H, W, D, argmax);
+}
+void launch_wta_diag(cudaStream_t s, const float *vol, uint16_t *raw, int *row_last, int H, int W, int D) {
+    k_wta_diag<<<dim3((W + kDiagT - 1) / kDiagT, H), kDiagT, 0, s>>>(vol, raw, row_last, W, D);
 }
 void launch_wta_fill(cudaStream_t s, const uint16_t *raw, const int *row_last, uint8_t *out, int H, int W,
                      int mirror) {

@@ -33,6 +33,7 @@ enum Slot {
     SL_V_RAW, SL_V_ROWLAST, SL_V_DISP,      // WTA winners, row summaries, view disparities
     SL_V_MEAN, SL_V_REC,                    // NCC means, fused-path pixel records
     SL_V_MED,                               // median-filtered arm images
+    SL_V_FINAL,                             // the left view's final volume (FP16 form, shared right view)
     SL_BATCH0, SL_BATCH1, SL_BATCH2, SL_BATCH3,
     SL_COUNT
 };
@@ -204,6 +205,9 @@ void launch_wta_local(cudaStream_t s, const float *cost, uint16_t *raw, int *row
                       int argmax);
 void launch_wta_fill(cudaStream_t s, const uint16_t *raw, const int *row_last, uint8_t *out, int H, int W,
                      int mirror);
+// the right view's winners from the left view's final volume [H][W][D] (its
+// diagonals (x + d mod W, d)); raw / row_last in the right view's mirrored columns
+void launch_wta_diag(cudaStream_t s, const float *vol, uint16_t *raw, int *row_last, int H, int W, int D);
 void launch_cross_check(cudaStream_t s, const uint8_t *dl, const uint8_t *dr, uint8_t *mask, int H, int W);
 void launch_flip(cudaStream_t s, const uint8_t *in, uint8_t *out, int H, int W, int ch, int mirror);
 void launch_gray_to_rgb(cudaStream_t s, const uint8_t *g, uint8_t *rgb, long n);

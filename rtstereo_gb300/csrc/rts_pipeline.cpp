@@ -426,12 +426,39 @@ rts_status pipeline_device(rts_ctx *c, const rts_params &p, int H, int W, const 
     }
     if (!cost_out && p.aggr == RTS_AGGR_CROSS && cross_fused_supported(p))
         return pipeline_cross_views(c, p, H, W, lg, rg, lc, rc, dl, dr, mask);
+    // FP16 form, adaptive weights: the right view's final costs are the left view's
+    // read along diagonals (launch_wta_diag), so one aggregation serves both views.
+    // Not for NCC (an arg-max whose products are not symmetric in the two images).
+    const bool shared_right = p.right_view && p.precision == RTS_PREC_F16 && p.aggr == RTS_AGGR_AW &&
+                              p.cost1 != RTS_COST_NCC && p.cost2 != RTS_COST_NCC && fused_supported(p, H, W);
+    float *final_vol = cost_out;
+    if (shared_right && !final_vol) {
+        void *fv;
+        RTS_TRY(scratch(c, SL_V_FINAL, np * p.disp_range * 4, &fv));
+        final_vol = (float *)fv;
+    }
     {
         StageScope sc(c, "left_view");
         ViewIn v{lg, rg, lc, rc, ll, rl};
-        RTS_TRY(run_view(c, p, H, W, v, dl, 0, cost_out));
+        RTS_TRY(run_view(c, p, H, W, v, dl, 0, final_vol));
     }
     if (!p.right_view) return RTS_OK;
+    if (shared_right) {
+        void *raw, *rlast;
+        {
+            StageScope sc(c, "right_view");
+            RTS_TRY(scratch(c, SL_V_RAW, np * 2, &raw));
+            RTS_TRY(scratch(c, SL_V_ROWLAST, (size_t)H * 4, &rlast));
+            RTS_CU(c, cudaMemsetAsync(rlast, 0xff, (size_t)H * 4, s));
+            launch_wta_diag(s, final_vol, (uint16_t *)raw, (int *)rlast, H, W, p.disp_range);
+            launch_wta_fill(s, (const uint16_t *)raw, (const int *)rlast, dr, H, W, 1);
+            count_launch(c, 2);
+        }
+        StageScope sc(c, "cross_check");
+        launch_cross_check(s, dl, dr, mask, H, W);
+        count_launch(c);
+        return check_launch(c, "pipeline");
+    }
     // right view: mirrored copies (a few bytes per pixel next to the D floats per pixel of the view)
     void *gv, *cv = nullptr, *lv = nullptr;
     RTS_TRY(scratch(c, SL_V_GRAY, np * 2, &gv));

@@ -280,6 +280,33 @@ def test_golden_modules(ctx, golden):
         assert bits_equal(ctx.calcAWCostL2R(wl, wr, golden["aw/cost"], rad), golden[f"aw{rad}/l2r"])
 
 
+@pytest.mark.parametrize("W,H,D,rad", [(96, 20, 40, 5), (300, 40, 64, 16), (40, 9, 40, 3)])
+def test_fp16_aw_right_view_from_left_volume(ctx, oracle_mod, W, H, D, rad):
+    """FP16 form, adaptive weights: the right view's winners are the arg-min of the
+    left view's final volume along the diagonals (x + d mod W, d), with the
+    reference's carry, in the right view's mirrored raster order."""
+    import rtstereo_gb300 as R
+    O = oracle_mod
+    L, Rr = synth(W + 3 * H + D, W, H, D, 4)
+    Lc, Rc = R.gray_to_rgb(L), R.gray_to_rgb(Rr)
+    lab = (R.rgb_to_lab(Lc), R.rgb_to_lab(Rc))
+    g = ctx.pipeline(R.params(disp_range=D, aggr=2, aw_rad=rad, precision=R.PREC_F16), L, Rr, Lc, Rc, *lab,
+                     want_cost=True)
+    vol = g[3]
+    assert bits_equal(g[1], diag_right_view(O, vol)), "right disparity"
+    assert bits_equal(g[0], O.wta(vol)), "left disparity"
+    assert bits_equal(g[2], O.cross_check(g[0], g[1])), "cross-check mask"
+
+
+def diag_right_view(O, vol):
+    """The right view's disparities from the left view's final volume: WTA (with
+    the carry, in the right view's mirrored raster order) over (x + d mod W, d)."""
+    H, W, D = vol.shape
+    xm, d = np.arange(W), np.arange(D)
+    cols = ((W - 1 - xm)[:, None] + d[None, :]) % W
+    return np.ascontiguousarray(O.wta(np.ascontiguousarray(vol[:, cols, d[None, :]]))[:, ::-1])
+
+
 @pytest.mark.parametrize("kw", [dict(disp_range=64, aggr=3), dict(disp_range=48, aggr=2, aw_rad=16)])
 def test_fp16_form_agrees_with_plain(ctx, kw):
     """FP16 storage (fp32 accumulation): most disparities equal the plain form's."""
