@@ -84,28 +84,45 @@ __global__ void k_cost_volume(const uint4 *__restrict__ rr, const uint4 *__restr
 
 // AD (optionally truncated) + census combined through the two host tables, the
 // integer path: warp per pixel, lane = disparity, so the reference record is a
-// broadcast and the target records and the volume row are contiguous.
+// broadcast and the volume row is contiguous.  Block per (row, 64 pixels): the
+// target records the block meets, columns x0 - D + 1 .. x0 + 63 (wrapped as in
+// seq/PixelBasedCost.cpp:19-20), and the two tables are staged in shared memory
+// once, so an entry reads its target record (consecutive lanes, consecutive
+// records) and its two table values from shared memory.
 constexpr int kAdcPx = 8;
+constexpr int kAdcTX = 8 * kAdcPx;          // pixels of a block
+constexpr int kAdcL1 = 768, kAdcL2 = 68;    // table entries staged: AD <= 765, census <= 64
 template <typename T>
 __global__ void __launch_bounds__(256) k_cost_volume_adc(const uint4 *__restrict__ rr, const uint4 *__restrict__ rt,
                                                         T *__restrict__ vol, int H, int W, int D, int itrunc,
                                                         const float *__restrict__ lut1, const float *__restrict__ lut2) {
-    // a warp takes kAdcPx consecutive pixels of the row (fewer, larger blocks)
-    const int y = blockIdx.y, lane = threadIdx.x & 31;
-    const int xw = (blockIdx.x * 8 + (threadIdx.x >> 5)) * kAdcPx;
+    __shared__ uint4 trec[kAdcTX + 255];  // D <= 256
+    __shared__ float t1[kAdcL1], t2[kAdcL2];
+    const int y = blockIdx.y, lane = threadIdx.x & 31, tid = threadIdx.x;
+    const int x0 = blockIdx.x * kAdcTX, base = x0 - D + 1;
     const uint4 *trow = rt + (size_t)y * W;
+    for (int i = tid; i < kAdcTX + D - 1; i += 256) {
+        int xt = base + i;
+        if (xt < 0) xt += W;  // seq/PixelBasedCost.cpp:19-20 (D <= W)
+        trec[i] = trow[imin(xt, W - 1)];  // columns past the row end are never read
+    }
+    for (int i = tid; i < kAdcL1; i += 256) t1[i] = lut1[i];
+    if (tid < kAdcL2) t2[tid] = lut2[tid];
+    __syncthreads();
+    // a warp takes kAdcPx consecutive pixels of the row
+    const int xw = x0 + (tid >> 5) * kAdcPx;
 #pragma unroll 2
     for (int i = 0; i < kAdcPx; i++) {
         const int x = xw + i;
         if (x >= W) return;
         const uint4 a = rr[(size_t)y * W + x];
         T *out = vol + ((size_t)y * W + x) * D;
+        const uint4 *tb = trec + (x - base);  // target of disparity d: tb[-d]
         for (int d = lane; d < D; d += 32) {
-            const int xt = x - d < 0 ? x - d + W : x - d;  // seq/PixelBasedCost.cpp:19-20
-            const uint4 b = trow[xt];
+            const uint4 b = tb[-d];
             const int sad = imin((int)__vsadu4(a.z, b.z), itrunc);    // seq/PixelBasedCost.cpp:86-91 / :106-112
             const int ham = __popc(a.x ^ b.x) + __popc(a.y ^ b.y);   // seq/CensusTransform.cpp:52-60
-            out[d] = to_store<T>(__fadd_rn(__ldg(lut1 + sad), __ldg(lut2 + ham)));  // seq/CombineCost.cpp:23
+            out[d] = to_store<T>(__fadd_rn(t1[sad], t2[ham]));       // seq/CombineCost.cpp:23
         }
     }
 }
@@ -787,7 +804,7 @@ rts_status cost_volume_fast(rts_ctx *c, const rts_params &p, int H, int W, const
     RTS_TRY(cost_cfg(c, p, &cfg));
     const int D = p.disp_range;
     if (cfg.int_path && cfg.k1 == RTS_COST_AD && cfg.k2 == RTS_COST_CENSUS) {
-        const dim3 g((unsigned)((W + 8 * kAdcPx - 1) / (8 * kAdcPx)), H);
+        const dim3 g((unsigned)((W + kAdcTX - 1) / kAdcTX), H);
         if (half) k_cost_volume_adc<__half><<<g, 256, 0, c->stream>>>(rr, rt, (__half *)vol, H, W, D, cfg.itrunc, cfg.lut1, cfg.lut2);
         else k_cost_volume_adc<float><<<g, 256, 0, c->stream>>>(rr, rt, (float *)vol, H, W, D, cfg.itrunc, cfg.lut1, cfg.lut2);
         count_launch(c);
