@@ -854,6 +854,8 @@ NCU_BOX_BYTES = {(1920, 1080, 128, 4): 1.1375e9}
 def roofline(stages, name, W, H, D, ag, peaks, src, p, ms_pair=None, sms=152):
     """Dominant kernel: algorithmic work per launch / its CUDA-event time, against
     the measured peak; traffic = DRAM bytes per launch from ncu."""
+    # left_view / right_view are scopes around a view's stages, not kernels
+    stages = {k: v for k, v in stages.items() if k not in ("left_view", "right_view")}
     if not stages:
         return None
     dom = max(stages.items(), key=lambda kv: kv[1][1])

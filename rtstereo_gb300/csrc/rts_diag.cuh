@@ -42,11 +42,16 @@ __device__ __forceinline__ void wta_diag_item(const float *__restrict__ vol, uin
     for (int c = 0; 32 * c < D; c++) {
         const int d = 32 * c + lane;
         float v[NI];
+        // column of staged row i = warp + 8k: one modulo per chunk, then steps of 8
+        // wrapped by a subtraction (W >= 8), or by the modulo for narrower images
+        int col = (x0 + 32 * c + warp) % W;
 #pragma unroll
         for (int k = 0; k < NI; k++) {
             const int i = warp + (kDiagT / 32) * k;
             v[k] = 0.f;
-            if (i < kDiagRows && d < D) v[k] = row[(size_t)((x0 + 32 * c + i) % W) * D + d];
+            if (i < kDiagRows && d < D) v[k] = row[(size_t)col * D + d];
+            col += kDiagT / 32;
+            col = col >= W ? (W >= kDiagT / 32 ? col - W : col % W) : col;
         }
         __syncthreads();  // the previous chunk's readers are done
 #pragma unroll

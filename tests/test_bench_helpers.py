@@ -44,6 +44,10 @@ def test_roofline_fields():
                          R.params(aggr=2, disp_range=64, precision=R.PREC_F16), sms=160)
     assert r16["peak"] == pytest.approx(160 * 128 * 2000e6 / 1e12) and "160 SMs" in r16["peak_source"]
     assert r16["ops_per_launch"] == pytest.approx(3 * 33 * 33 * 640 * 480 * 64)
+    # the FP16 form aggregates once: the left-view scope around it is not a kernel
+    r16 = bench.roofline({"left_view": (1, 3.3), "aw_wta": (1, 3.2), "right_view": (1, 0.1)}, "aw_640x480_d64",
+                         640, 480, 64, 2, peaks, "measured", R.params(aggr=2, disp_range=64, precision=R.PREC_F16))
+    assert r16["kernel"] == "k_aw_wta_pipe" and r16["ms_per_launch"] == pytest.approx(3.2)
     # box: FP32-pipe bound, (2r+1)^2 adds per entry, one launch per view
     p = R.params(aggr=1, disp_range=128, box_rad=4)
     r = bench.roofline({"box_wta": (2, 2.0), "left_view": (1, 1.5)}, "box_1920x1080_d128", 1920, 1080, 128, 1,
