@@ -803,7 +803,7 @@ def run_ours(args, rank, world):
     bench = Bench(dev, world, args.steps, args.warmup)
     m = bench.measure(args.workload, args.precision)
     extra = {}
-    # the other spec figures ride on the default line (one GPU): the FP16 form,
+    # the other target figures ride on the default line (one GPU): the FP16 form,
     # the 1920x1080 cross-based pipeline, and the serving loop
     if world == 1 and args.workload == DEFAULT and args.precision == "f32" and not args.no_extra:
         peaks, _ = measured_peaks()

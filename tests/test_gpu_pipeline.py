@@ -280,7 +280,7 @@ def test_golden_modules(ctx, golden):
         assert bits_equal(ctx.calcAWCostL2R(wl, wr, golden["aw/cost"], rad), golden[f"aw{rad}/l2r"])
 
 
-@pytest.mark.parametrize("W,H,D,rad", [(96, 20, 40, 5), (300, 40, 64, 16), (40, 9, 40, 3)])
+@pytest.mark.parametrize("W,H,D,rad", [(96, 20, 40, 5), (300, 40, 64, 16), (40, 9, 40, 3), (52, 12, 36, 4)])
 def test_fp16_aw_right_view_from_left_volume(ctx, oracle_mod, W, H, D, rad):
     """FP16 form, adaptive weights: the right view's winners are the arg-min of the
     left view's final volume along the diagonals (x + d mod W, d), with the
