@@ -5,6 +5,9 @@
 // float adds in window order, no fused multiply-add), so their results are
 // bit-identical to the reference on the same inputs.  The fused pipeline
 // kernels in k_pipe.cu keep the same per-entry order with tiled data reuse.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include "rts_common.cuh"
 
 namespace rts {
@@ -238,16 +241,67 @@ __device__ __forceinline__ void box_dp_tile(const float2 *bt2, unsigned long lon
     }
 }
 
+// Tiles whose window rows and columns all lie inside the image (no wrap) arrive
+// by one TMA copy: the volume as a 3-D tensor (d, x, y) of f32, box
+// (64, TW, TH) at (64 z, x0 - R, y0 - R), written densely in the [TH][TW][64]
+// order the sums read, disparities past D filled with zeros; one thread issues
+// it and every thread waits on an mbarrier.  The wait is bounded: a copy that has
+// not landed after kTmaSpin polls counts in g_box_tma_timeouts and its block
+// writes nothing.  Border tiles (wrapped cells) take the cp.async staging.
+constexpr int kTmaSpin = 1 << 22;
+__device__ int g_box_tma_timeouts;
+
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+    for (int it = 0; it < kTmaSpin; it++) {
+        uint32_t done;
+        asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                     "selp.u32 %0, 1, 0, p;\n\t}"
+                     : "=r"(done)
+                     : "r"(bar), "r"(parity)
+                     : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
 // one tile per block
 template <int R, int POS>
-__global__ void __launch_bounds__(256, 2) k_box_best_dp(const float *__restrict__ vol,
+__global__ void __launch_bounds__(256, 2) k_box_best_dp(const __grid_constant__ CUtensorMap tmap, int use_tma,
+                                                        const float *__restrict__ vol,
                                                         unsigned long long *__restrict__ best, int H, int W, int D,
                                                         int argmax, float rcp_area) {
-    extern __shared__ float2 bt2[];  // [TH][TW][32] pairs
+    constexpr int TW = kBoxDpTX + 2 * R, TH = kBoxDpTY + 2 * R;
+    constexpr uint32_t kBytes = (uint32_t)TW * TH * 64 * sizeof(float);
+    extern __shared__ __align__(128) float2 bt2[];  // [TH][TW][32] pairs
+    __shared__ __align__(8) uint64_t bar;
     const int x0 = blockIdx.x * kBoxDpTX, y0 = blockIdx.y * kBoxDpTY, d = blockIdx.z * 64 + 2 * (threadIdx.x & 31);
-    box_dp_stage<R>(bt2, vol, H, W, D, x0, y0, d);
-    asm volatile("cp.async.wait_all;\n" ::: "memory");
-    __syncthreads();
+    const bool tma = use_tma && x0 >= R && x0 + kBoxDpTX + R <= W && y0 >= R && y0 + kBoxDpTY + R <= H;
+    if (tma) {
+        const uint32_t ba = (uint32_t)__cvta_generic_to_shared(&bar);
+        if (threadIdx.x == 0) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(ba) : "memory");
+            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            const uint32_t dst = (uint32_t)__cvta_generic_to_shared(bt2);
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(ba), "r"(kBytes) : "memory");
+            asm volatile(
+                "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, "
+                "%4}], [%5];" ::"r"(dst),
+                "l"(reinterpret_cast<uint64_t>(&tmap)), "r"((int)blockIdx.z * 64), "r"(x0 - R), "r"(y0 - R), "r"(ba)
+                : "memory");
+        }
+        if (!mbar_wait(ba, 0)) {
+            if (threadIdx.x == 0) atomicAdd(&g_box_tma_timeouts, 1);
+            mbar_wait(ba, 0);  // the copy may still land in this block's shared memory
+            return;
+        }
+    } else {
+        box_dp_stage<R>(bt2, vol, H, W, D, x0, y0, d);
+        asm volatile("cp.async.wait_all;\n" ::: "memory");
+        __syncthreads();
+    }
     box_dp_tile<R, POS>(bt2, best, H, W, D, argmax, rcp_area, x0, y0, d);
 }
 
@@ -493,6 +547,32 @@ void launch_box(cudaStream_t s, const float *in, float *out, int H, int W, int D
     k_box<<<row_grid((long)W * D, H, 256), 256, 0, s>>>(in, out, H, W, D, r);
 }
 bool box_best_supported(int r) { return r >= 1 && r <= 8; }
+
+// The volume [H][W][D] f32 as a 3-D tensor map for k_box_best_dp's TMA tiles,
+// box (64 disparities, bw pixels, bh rows).  False (cp.async staging for every
+// tile) where the layout breaks a TMA rule: rows of D floats must be a multiple
+// of 16 bytes and the base 16-byte aligned; or where the driver has no encoder.
+static bool box_tensor_map(CUtensorMap *m, const float *vol, int H, int W, int D, int bw, int bh) {
+    static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+    static bool tried = false;
+    if (!tried) {
+        tried = true;
+        void *fn = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            encode = (PFN_cuTensorMapEncodeTiled_v12000)fn;
+    }
+    if (!encode || D % 4 != 0 || ((uintptr_t)vol & 15) != 0) return false;
+    const cuuint64_t dims[3] = {(cuuint64_t)D, (cuuint64_t)W, (cuuint64_t)H};
+    const cuuint64_t strides[2] = {(cuuint64_t)D * 4, (cuuint64_t)W * D * 4};
+    const cuuint32_t box[3] = {64, (cuuint32_t)bw, (cuuint32_t)bh};
+    const cuuint32_t estr[3] = {1, 1, 1};
+    return encode(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float *>(vol), dims, strides, box, estr,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
 void launch_box_best(cudaStream_t s, const float *vol, unsigned long long *best, uint16_t *raw, int *row_last, int H,
                      int W, int D, int r, int argmax, int pos) {
     // disparity pairs for even D above one warp's 32; else a lane per disparity
@@ -509,7 +589,9 @@ void launch_box_best(cudaStream_t s, const float *vol, unsigned long long *best,
     auto go_dp = [&](auto kern, int R) {
         const size_t smem = (size_t)(kBoxDpTX + 2 * R) * (kBoxDpTY + 2 * R) * 64 * sizeof(float);
         cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        kern<<<g, 256, smem, s>>>(vol, best, H, W, D, argmax, rcp_area);
+        CUtensorMap tm{};
+        const int use_tma = box_tensor_map(&tm, vol, H, W, D, kBoxDpTX + 2 * R, kBoxDpTY + 2 * R) ? 1 : 0;
+        kern<<<g, 256, smem, s>>>(tm, use_tma, vol, best, H, W, D, argmax, rcp_area);
     };
 #define RTS_BOX(RR)                                                \
     case RR:                                                       \

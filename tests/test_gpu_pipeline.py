@@ -65,11 +65,13 @@ def test_cost_aggregation_matrix(ctx, oracle_mod, W, H, D, aggr):
 
 
 @pytest.mark.parametrize("W,H,D,rad", [(70, 19, 48, 4), (33, 9, 16, 1), (96, 40, 32, 8), (45, 30, 40, 3),
-                                       (150, 23, 130, 8), (40, 11, 34, 5), (72, 9, 64, 1)])
+                                       (150, 23, 130, 8), (40, 11, 34, 5), (72, 9, 64, 1), (120, 60, 68, 8),
+                                       (100, 40, 96, 2)])
 @pytest.mark.parametrize("c1,c2", [(1, 3), (3, 0), (5, 0)])
 def test_box_fused_matches_oracle(ctx, oracle_mod, W, H, D, rad, c1, c2):
     # without a cost volume out the box runs as one box + arg-min pass (arg-max for NCC);
-    # even D above 32 takes the disparity-pair kernel (ragged last block at D = 34, 130)
+    # even D above 32 takes the disparity-pair kernel (ragged last block at D = 34, 130),
+    # whose inner tiles arrive by TMA when D is a multiple of 4 (48, 40, 64, 68, 96)
     L, Rr = synth(W * 7 + H + rad, W, H, D, 3)
     g, o = run_both(ctx, oracle_mod, L, Rr, disp_range=D, cost1=c1, cost2=c2, aggr=1, box_rad=rad, ncc_hrad=2,
                     ncc_wrad=2)
