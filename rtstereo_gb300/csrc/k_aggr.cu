@@ -5,10 +5,8 @@
 // float adds in window order, no fused multiply-add), so their results are
 // bit-identical to the reference on the same inputs.  The fused pipeline
 // kernels in k_pipe.cu keep the same per-entry order with tiled data reuse.
-#include <cuda.h>
-#include <cudaTypedefs.h>
-
 #include "rts_common.cuh"
+#include "rts_tma.h"
 
 namespace rts {
 
@@ -248,21 +246,7 @@ __device__ __forceinline__ void box_dp_tile(const float2 *bt2, unsigned long lon
 // it and every thread waits on an mbarrier.  The wait is bounded: a copy that has
 // not landed after kTmaSpin polls counts in g_box_tma_timeouts and its block
 // writes nothing.  Border tiles (wrapped cells) take the cp.async staging.
-constexpr int kTmaSpin = 1 << 22;
 __device__ int g_box_tma_timeouts;
-
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
-    for (int it = 0; it < kTmaSpin; it++) {
-        uint32_t done;
-        asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-                     "selp.u32 %0, 1, 0, p;\n\t}"
-                     : "=r"(done)
-                     : "r"(bar), "r"(parity)
-                     : "memory");
-        if (done) return true;
-    }
-    return false;
-}
 
 // one tile per block
 template <int R, int POS>
@@ -272,26 +256,20 @@ __global__ void __launch_bounds__(256, 2) k_box_best_dp(const __grid_constant__ 
                                                         int argmax, float rcp_area) {
     constexpr int TW = kBoxDpTX + 2 * R, TH = kBoxDpTY + 2 * R;
     constexpr uint32_t kBytes = (uint32_t)TW * TH * 64 * sizeof(float);
-    extern __shared__ __align__(128) float2 bt2[];  // [TH][TW][32] pairs
+    // [TH][TW][32] pairs; a TMA destination must be 128-byte aligned (checked below:
+    // a block whose buffer is not stages by cp.async)
+    extern __shared__ __align__(128) float2 bt2[];
     __shared__ __align__(8) uint64_t bar;
     const int x0 = blockIdx.x * kBoxDpTX, y0 = blockIdx.y * kBoxDpTY, d = blockIdx.z * 64 + 2 * (threadIdx.x & 31);
-    const bool tma = use_tma && x0 >= R && x0 + kBoxDpTX + R <= W && y0 >= R && y0 + kBoxDpTY + R <= H;
+    const bool tma = use_tma && x0 >= R && x0 + kBoxDpTX + R <= W && y0 >= R && y0 + kBoxDpTY + R <= H &&
+                     ((uint32_t)__cvta_generic_to_shared(bt2) & 127) == 0;
     if (tma) {
         const uint32_t ba = (uint32_t)__cvta_generic_to_shared(&bar);
-        if (threadIdx.x == 0) {
-            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(ba) : "memory");
-            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        }
+        if (threadIdx.x == 0) mbar_init(ba);
         __syncthreads();
-        if (threadIdx.x == 0) {
-            const uint32_t dst = (uint32_t)__cvta_generic_to_shared(bt2);
-            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(ba), "r"(kBytes) : "memory");
-            asm volatile(
-                "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, "
-                "%4}], [%5];" ::"r"(dst),
-                "l"(reinterpret_cast<uint64_t>(&tmap)), "r"((int)blockIdx.z * 64), "r"(x0 - R), "r"(y0 - R), "r"(ba)
-                : "memory");
-        }
+        if (threadIdx.x == 0)
+            tma_load_3d((uint32_t)__cvta_generic_to_shared(bt2), &tmap, (int)blockIdx.z * 64, x0 - R, y0 - R, ba,
+                        kBytes);
         if (!mbar_wait(ba, 0)) {
             if (threadIdx.x == 0) atomicAdd(&g_box_tma_timeouts, 1);
             mbar_wait(ba, 0);  // the copy may still land in this block's shared memory
@@ -548,31 +526,6 @@ void launch_box(cudaStream_t s, const float *in, float *out, int H, int W, int D
 }
 bool box_best_supported(int r) { return r >= 1 && r <= 8; }
 
-// The volume [H][W][D] f32 as a 3-D tensor map for k_box_best_dp's TMA tiles,
-// box (64 disparities, bw pixels, bh rows).  False (cp.async staging for every
-// tile) where the layout breaks a TMA rule: rows of D floats must be a multiple
-// of 16 bytes and the base 16-byte aligned; or where the driver has no encoder.
-static bool box_tensor_map(CUtensorMap *m, const float *vol, int H, int W, int D, int bw, int bh) {
-    static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
-    static bool tried = false;
-    if (!tried) {
-        tried = true;
-        void *fn = nullptr;
-        cudaDriverEntryPointQueryResult q;
-        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) ==
-                cudaSuccess &&
-            q == cudaDriverEntryPointSuccess)
-            encode = (PFN_cuTensorMapEncodeTiled_v12000)fn;
-    }
-    if (!encode || D % 4 != 0 || ((uintptr_t)vol & 15) != 0) return false;
-    const cuuint64_t dims[3] = {(cuuint64_t)D, (cuuint64_t)W, (cuuint64_t)H};
-    const cuuint64_t strides[2] = {(cuuint64_t)D * 4, (cuuint64_t)W * D * 4};
-    const cuuint32_t box[3] = {64, (cuuint32_t)bw, (cuuint32_t)bh};
-    const cuuint32_t estr[3] = {1, 1, 1};
-    return encode(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float *>(vol), dims, strides, box, estr,
-                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
-}
 void launch_box_best(cudaStream_t s, const float *vol, unsigned long long *best, uint16_t *raw, int *row_last, int H,
                      int W, int D, int r, int argmax, int pos) {
     // disparity pairs for even D above one warp's 32; else a lane per disparity
@@ -590,7 +543,7 @@ void launch_box_best(cudaStream_t s, const float *vol, unsigned long long *best,
         const size_t smem = (size_t)(kBoxDpTX + 2 * R) * (kBoxDpTY + 2 * R) * 64 * sizeof(float);
         cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         CUtensorMap tm{};
-        const int use_tma = box_tensor_map(&tm, vol, H, W, D, kBoxDpTX + 2 * R, kBoxDpTY + 2 * R) ? 1 : 0;
+        const int use_tma = volume_tensor_map(&tm, vol, H, W, D, 4, 64, kBoxDpTX + 2 * R, kBoxDpTY + 2 * R) ? 1 : 0;
         kern<<<g, 256, smem, s>>>(tm, use_tma, vol, best, H, W, D, argmax, rcp_area);
     };
 #define RTS_BOX(RR)                                                \

@@ -197,15 +197,19 @@ __global__ void k_window_mean(const uint8_t *__restrict__ img, float *__restrict
 // in tap (raster) order, the cell written only when den != 0.  Over tiles: block per (row y, 64 pixels,
 // 64 disparities), each thread 4 pixels x 4 disparities.  Per chunk of taps the
 // block stages, in tap (raster) order, {rv, rv*rv} of its 64 reference pixels and
-// {tv, tv} of the 127 target columns t = x - d it meets (rv = I - mean, tv likewise,
+// tv of the 127 target columns t = x - d it meets (rv = I - mean, tv likewise,
 // seq/NCCDisparity.cpp:55-62).  An entry's (nom, den) pair then takes per tap
-//   (rv*tv, (rv*rv)*tv) = packed multiply of {rv, rv*rv} by {tv, tv},
-//   den term = ((rv*rv)*tv)*tv, (nom, den) += (rv*tv, den term)   (packed add)
-// which are the reference's operations in its order.
+//   rv*tv, ((rv*rv)*tv)*tv as scalar products, (nom, den) += (rv*tv, den term)
+//   (one packed add)
+// which are the reference's operations in its order.  A thread's 16 entries read
+// 8 reference and 8 target floats per tap: four 16-byte shared loads, the
+// target values held once (a {tv, tv} pair for a packed multiply would double
+// the shared-memory traffic, which bounds the loop).
 constexpr int kNccTX = 64, kNccTD = 64, kNccTaps = 49;
-// Shared rows hold float2 values in 16-byte chunks; chunk c is stored at
+// Reference rows hold float2 values in 16-byte chunks; chunk c is stored at
 // c ^ ((c >> 3) & 1), so the eight 16-byte reads of a quarter warp (4 pixels
-// apart) fall in distinct banks.
+// apart) fall in distinct banks.  A quarter warp's target reads are eight
+// consecutive 16-byte chunks.
 __device__ __forceinline__ int ncc_swz(int u) { return (((u >> 1) ^ ((u >> 4) & 1)) << 1) | (u & 1); }
 
 __global__ void __launch_bounds__(256) k_ncc_tiled(const uint8_t *__restrict__ ref, const uint8_t *__restrict__ tar,
@@ -214,7 +218,7 @@ __global__ void __launch_bounds__(256) k_ncc_tiled(const uint8_t *__restrict__ r
     constexpr int NT = kNccTX + kNccTD - 1;       // target columns of a tile
     extern __shared__ __align__(16) unsigned char nsm[];
     float2 (*rq)[kNccTX] = reinterpret_cast<float2 (*)[kNccTX]>(nsm);                         // {rv, rv*rv}
-    float2 (*tq)[NT + 1] = reinterpret_cast<float2 (*)[NT + 1]>(nsm + sizeof(float2) * kNccTaps * kNccTX);  // {tv, tv}
+    float (*tq)[NT + 1] = reinterpret_cast<float (*)[NT + 1]>(nsm + sizeof(float2) * kNccTaps * kNccTX);  // tv
     const int tid = threadIdx.x;
     const int px0 = 4 * (tid & 15), d0 = 4 * (tid >> 4);
     const int y = blockIdx.y, x0 = blockIdx.x * kNccTX, dc0 = blockIdx.z * kNccTD;
@@ -222,11 +226,11 @@ __global__ void __launch_bounds__(256) k_ncc_tiled(const uint8_t *__restrict__ r
     const int ew = 2 * wr + 1, taps = (2 * hr + 1) * ew;
     // the tap offsets {dy, dx} of a chunk, made once per chunk
     __shared__ int2 tapoff[kNccTaps];
-    unsigned long long acc[4][4];  // (nom, den) of pixel px0 + j, disparity d0 + i
+    float2 acc[4][4];  // (nom, den) of pixel px0 + j, disparity d0 + i
 #pragma unroll
     for (int j = 0; j < 4; j++)
 #pragma unroll
-        for (int i = 0; i < 4; i++) acc[j][i] = 0ull;
+        for (int i = 0; i < 4; i++) acc[j][i] = make_float2(0.f, 0.f);
     for (int k0 = 0; k0 < taps; k0 += kNccTaps) {
         const int nk = min(kNccTaps, taps - k0);
         __syncthreads();  // the previous chunk is consumed
@@ -256,7 +260,7 @@ __global__ void __launch_bounds__(256) k_ncc_tiled(const uint8_t *__restrict__ r
             for (int k = tid < NT ? 0 : 1; k < nk; k += 2) {
                 const int2 to = tapoff[k];
                 const float tv = __fsub_rn((float)tar[(size_t)wrap1(y + to.x, H) * W + wrap1(t + to.y, W)], mt);
-                tq[k][ncc_swz(u)] = make_float2(tv, tv);
+                tq[k][u] = tv;
             }
         }
         __syncthreads();
@@ -264,23 +268,26 @@ __global__ void __launch_bounds__(256) k_ncc_tiled(const uint8_t *__restrict__ r
         const int ub = px0 - d0 + kNccTD - 4;
 #pragma unroll 7
         for (int k = 0; k < nk; k++) {
-            unsigned long long r[4], tt[8];
-            const ulonglong2 ra = *reinterpret_cast<const ulonglong2 *>(&rq[k][ncc_swz(px0)]);
-            const ulonglong2 rb = *reinterpret_cast<const ulonglong2 *>(&rq[k][ncc_swz(px0 + 2)]);
-            r[0] = ra.x; r[1] = ra.y; r[2] = rb.x; r[3] = rb.y;
-#pragma unroll
-            for (int m = 0; m < 4; m++) {
-                const ulonglong2 v = *reinterpret_cast<const ulonglong2 *>(&tq[k][ncc_swz(ub + 2 * m)]);
-                tt[2 * m] = v.x;
-                tt[2 * m + 1] = v.y;
-            }
+            float2 r[4];
+            float tt[8];
+            const float4 ra = *reinterpret_cast<const float4 *>(&rq[k][ncc_swz(px0)]);
+            const float4 rb = *reinterpret_cast<const float4 *>(&rq[k][ncc_swz(px0 + 2)]);
+            r[0] = make_float2(ra.x, ra.y); r[1] = make_float2(ra.z, ra.w);
+            r[2] = make_float2(rb.x, rb.y); r[3] = make_float2(rb.z, rb.w);
+            const float4 ta = *reinterpret_cast<const float4 *>(&tq[k][ub]);
+            const float4 tb = *reinterpret_cast<const float4 *>(&tq[k][ub + 4]);
+            tt[0] = ta.x; tt[1] = ta.y; tt[2] = ta.z; tt[3] = ta.w;
+            tt[4] = tb.x; tt[5] = tb.y; tt[6] = tb.z; tt[7] = tb.w;
 #pragma unroll
             for (int j = 0; j < 4; j++)
 #pragma unroll
                 for (int i = 0; i < 4; i++) {
-                    const unsigned long long pr = mul2(r[j], tt[j - i + 3]);  // (rv*tv, (rv*rv)*tv)
-                    const float dt = __fmul_rn(half2_of(pr, 1), half2_of(tt[j - i + 3], 0));
-                    acc[j][i] = add2(acc[j][i], pack2(half2_of(pr, 0), dt));
+                    // scalar IEEE products (a product feeding a packed add stays unfused), the
+                    // pair (rv*tv, ((rv*rv)*tv)*tv) added by one packed add
+                    const float tv = tt[j - i + 3];
+                    const float nt = __fmul_rn(r[j].x, tv);
+                    const float dt = __fmul_rn(__fmul_rn(r[j].y, tv), tv);
+                    acc[j][i] = __fadd2_rn(acc[j][i], make_float2(nt, dt));
                 }
         }
     }
@@ -290,8 +297,8 @@ __global__ void __launch_bounds__(256) k_ncc_tiled(const uint8_t *__restrict__ r
         for (int i = 0; i < 4; i++) {
             const int x = x0 + px0 + j, d = dc0 + d0 + i;
             if (x < W && d < D) {
-                const float den = __fsqrt_rn(half2_of(acc[j][i], 1));  // seq/NCCDisparity.cpp:69
-                if (den != 0.f) cost[((size_t)y * W + x) * D + d] = __fdiv_rn(half2_of(acc[j][i], 0), den);
+                const float den = __fsqrt_rn(acc[j][i].y);  // seq/NCCDisparity.cpp:69
+                if (den != 0.f) cost[((size_t)y * W + x) * D + d] = __fdiv_rn(acc[j][i].x, den);
             }
         }
 }
@@ -396,7 +403,7 @@ void launch_window_mean(cudaStream_t s, const uint8_t *img, float *mean, int H, 
 void launch_ncc(cudaStream_t s, const uint8_t *ref, const uint8_t *tar, const float *mref, const float *mtar,
                 float *cost, int D, int H, int W, int hr, int wr) {
     const dim3 g((W + kNccTX - 1) / kNccTX, H, (D + kNccTD - 1) / kNccTD);
-    const size_t smem = sizeof(float2) * kNccTaps * (kNccTX + kNccTX + kNccTD);
+    const size_t smem = sizeof(float2) * kNccTaps * kNccTX + sizeof(float) * kNccTaps * (kNccTX + kNccTD);
     cudaFuncSetAttribute(k_ncc_tiled, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     k_ncc_tiled<<<g, 256, smem, s>>>(ref, tar, mref, mtar, cost, D, H, W, hr, wr);
 }
