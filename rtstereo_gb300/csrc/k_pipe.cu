@@ -16,6 +16,7 @@
 
 #include "rts_fused.cuh"
 #include "rts_pipe.h"
+#include "rts_tma.h"
 
 namespace rts {
 
@@ -406,8 +407,11 @@ __global__ void __launch_bounds__(kAwThreads, 3) k_aw_wta(const CT *__restrict__
 // otherwise (FP16 form, f16 volume staged as f16, D a multiple of 8) one FMA.
 // E: the window edge as a constant (33, the reference driver's 33 x 33 window), so
 // that the tap loop unrolls whole, or 0 for the edge of the e argument.
+__device__ int g_aw_tma_timeouts;
+
 template <typename CT, bool EXACT, int E>
-__global__ void __launch_bounds__(kAwThreads, 2) k_aw_wta_pipe(const CT *__restrict__ vol,
+__global__ void __launch_bounds__(kAwThreads, 2) k_aw_wta_pipe(const __grid_constant__ CUtensorMap tmap, int use_tma,
+                                                          const CT *__restrict__ vol,
                                                           const uint32_t *__restrict__ labr,
                                                           const uint32_t *__restrict__ labt,
                                                           const float *__restrict__ pw, const float *__restrict__ G,
@@ -425,16 +429,23 @@ __global__ void __launch_bounds__(kAwThreads, 2) k_aw_wta_pipe(const CT *__restr
     const float2 z2 = make_float2(zero, zero);
     constexpr int NT = kAwTX + kAwDC - 1;  // target columns of a tile
     constexpr int NTP = NT + 1;
-    // cost rows: kAwCPitch floats, or kAwHPitch halves (16-byte rows for the copies)
-    constexpr int CP = sizeof(CT) == 4 ? kAwCPitch : kAwHPitch;
+    // cost rows: 64 floats (dense, as a TMA copy writes them), or kAwHPitch halves
+    // (16-byte rows for the copies, the pitch keeping a half warp's rows apart in banks)
+    constexpr int CP = sizeof(CT) == 4 ? kAwDC : kAwHPitch;
     const int CS = (kAwTX + 2 * r + 4) * CP * (int)sizeof(CT) / 4;  // floats of one cost buffer
-    extern __shared__ __align__(16) float asm_[];
+    // no static shared memory: the dynamic buffers begin at the block's shared base,
+    // as a TMA destination must be 128-byte aligned (checked below all the same)
+    extern __shared__ __align__(128) float asm_[];
     // buffer b: costs at asm_ + b CS, reference weights at wR0 + b e 64, target weights at wT0 + b e NTP
     float *const wR0 = asm_ + 2 * CS, *const wT0 = wR0 + 2 * e * kAwTX;
     uint32_t *labbase = reinterpret_cast<uint32_t *>(asm_ + 2 * CS + 2 * e * kAwTX + 2 * e * NTP);
     const int LRN = kAwTX + 2 * r, LTN = NT + 2 * r;  // words of a reference / target Lab row
-    __shared__ float best_v[kAwTX];
-    __shared__ int best_i[kAwTX];
+    float *const best_v = reinterpret_cast<float *>(labbase + 3 * (LRN + LTN));  // [kAwTX]
+    int *const best_i = reinterpret_cast<int *>(best_v + kAwTX);                  // [kAwTX]
+    // plain form, tiles whose cost columns need no wrap: each tap row's cost rows arrive
+    // by one TMA copy (box 64 disparities x (64 + 2r) columns) completing on cbar[buffer]
+    uint64_t *const cbar =
+        reinterpret_cast<uint64_t *>((reinterpret_cast<uintptr_t>(best_i + kAwTX) + 7) & ~uintptr_t(7));  // [2]
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     constexpr int NW = kAwThreads / 32;
@@ -452,6 +463,23 @@ __global__ void __launch_bounds__(kAwThreads, 2) k_aw_wta_pipe(const CT *__restr
         best_i[tid] = 0x7fffffff;
     }
     const bool vec = (D & 3) == 0;
+    const bool tma_tile = sizeof(CT) == 4 && use_tma && x0 - r >= 0 && x0 + kAwTX + r <= W &&
+                          ((uint32_t)__cvta_generic_to_shared(asm_) & 127) == 0;
+    const uint32_t cb0 = (uint32_t)__cvta_generic_to_shared(cbar);
+    uint32_t cphase = 0;  // bit b: parity of the next completion of cbar[b]
+    if (tma_tile && tid == 0) {
+        mbar_init(cb0);
+        mbar_init(cb0 + 8);
+    }
+    // (the barriers' initialisation is published by the chunk loop's first __syncthreads)
+    auto cost_wait = [&](int b) {
+        if (!tma_tile) return;
+        if (!mbar_wait(cb0 + 8 * b, (cphase >> b) & 1)) {
+            if (tid == 0) atomicAdd(&g_aw_tma_timeouts, 1);
+            mbar_wait(cb0 + 8 * b, (cphase >> b) & 1);  // the copy may still land in this buffer
+        }
+        cphase ^= 1u << b;
+    };
 
     for (int dc0 = 0; dc0 < D; dc0 += kAwDC) {
         // sums of disparity pairs (dd0 + 2h, dd0 + 2h + 1) of pixel px0 + j, as float2 for
@@ -479,9 +507,16 @@ __global__ void __launch_bounds__(kAwThreads, 2) k_aw_wta_pipe(const CT *__restr
 
         // cost rows of tap row ky into C by cp.async (zero fill past D); wrapped
         // columns as in k_aw_wta (seq/AdaptiveWeightAggregation.cpp:95-97)
-        auto stage_cost = [&](int ky, float *C) {
+        auto stage_cost = [&](int ky, int b) {
+            float *C = asm_ + b * CS;
             const size_t crow = (size_t)(y + ky) * W;
             const uint32_t cbase = (uint32_t)__cvta_generic_to_shared(C);
+            if (tma_tile) {
+                if (tid == 0)
+                    tma_load_3d(cbase, &tmap, dc0, x0 - r, y + ky, cb0 + 8 * b,
+                                (uint32_t)((kAwTX + 2 * r) * kAwDC * sizeof(float)));
+                return;
+            }
             if constexpr (sizeof(CT) == 2) {
                 // f16 volume: 16-byte copies of 8 disparities (D is a multiple of 8)
                 for (int q = tid; q < (kAwTX + 2 * r) * (kAwDC / 8); q += kAwThreads) {
@@ -500,7 +535,7 @@ __global__ void __launch_bounds__(kAwThreads, 2) k_aw_wta_pipe(const CT *__restr
                     const int xs = imin(imax(wrap1(x0 - r + xi, W), 0), W - 1);
                     const int dg = dc0 + d4;
                     const float *src = vol + (crow + xs) * D + (dg < D ? dg : 0);
-                    const uint32_t dst = cbase + (uint32_t)((xi * kAwCPitch + d4) * 4);
+                    const uint32_t dst = cbase + (uint32_t)((xi * CP + d4) * 4);
                     asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(dst), "l"(src),
                                  "r"(dg < D ? 16 : 0)
                                  : "memory");
@@ -511,7 +546,7 @@ __global__ void __launch_bounds__(kAwThreads, 2) k_aw_wta_pipe(const CT *__restr
                     const int xs = imin(imax(wrap1(x0 - r + xi, W), 0), W - 1);
                     const int dg = dc0 + dd;
                     const float *src = vol + (crow + xs) * D + (dg < D ? dg : 0);
-                    const uint32_t dst = cbase + (uint32_t)((xi * kAwCPitch + dd) * 4);
+                    const uint32_t dst = cbase + (uint32_t)((xi * CP + dd) * 4);
                     asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(dst), "l"(src),
                                  "r"(dg < D ? 4 : 0)
                                  : "memory");
@@ -594,7 +629,7 @@ __global__ void __launch_bounds__(kAwThreads, 2) k_aw_wta_pipe(const CT *__restr
         __syncthreads();  // the previous chunk is done with every buffer
         stage_lab(ky_lo, 0);
         if (ky_lo + 1 <= ky_hi) stage_lab(ky_lo + 1, 1);
-        stage_cost(ky_lo, asm_);
+        stage_cost(ky_lo, 0);
         __syncthreads();
         for (int k = warp; k < e; k += NW) {
             Slice sl;
@@ -602,12 +637,13 @@ __global__ void __launch_bounds__(kAwThreads, 2) k_aw_wta_pipe(const CT *__restr
             slice_finish(sl, ky_lo, k, wR0, wT0);
         }
         asm volatile("cp.async.wait_all;\n" ::: "memory");
+        cost_wait(0);
         __syncthreads();
 
         for (int ky = ky_lo; ky <= ky_hi; ky++) {
             const int i = ky - ky_lo, b = i & 1;
             const bool next = ky + 1 <= ky_hi;
-            if (next) stage_cost(ky + 1, asm_ + (b ^ 1) * CS);
+            if (next) stage_cost(ky + 1, b ^ 1);
             if (ky + 2 <= ky_hi) stage_lab(ky + 2, (i + 2) % 3);
             const int lnext = (i + 1) % 3;
             const float *Cs = asm_ + b * CS, *wRs = wR0 + b * e * kAwTX, *wTs = wT0 + b * e * NTP;
@@ -712,6 +748,7 @@ __global__ void __launch_bounds__(kAwThreads, 2) k_aw_wta_pipe(const CT *__restr
                     slice_finish(sl, ky + 1, ks, wRn, wTn);
                 }
             asm volatile("cp.async.wait_all;\n" ::: "memory");
+            if (next) cost_wait(b ^ 1);
             __syncthreads();
         }
         // score / sum of weights (seq/AdaptiveWeightAggregation.cpp:108), staged for the arg-min
@@ -851,26 +888,32 @@ rts_status aw_fused(rts_ctx *c, const rts_params &p, int H, int W, const void *v
     // the pipelined kernel: two cost buffers (f32 rows, or f16 rows of 8-disparity
     // copies; their space also holds the [64][65] argmin staging), two weight
     // buffers, three Lab row pairs
+    // two cost buffers (their space also holds the [64][65] arg-min staging), two
+    // weight buffers, three Lab row pairs, the arg-min state and two mbarriers
     auto pipe_smem = [&](size_t row_bytes) {
         const size_t costs = 2 * (size_t)(kAwTX + 2 * r + 4) * row_bytes;
         return std::max(costs, (size_t)kAwTX * (kAwDC + 1) * 4) +
                sizeof(float) * (2 * (size_t)e * kAwTX + 2 * (size_t)e * (kAwTX + kAwDC)) +
-               sizeof(uint32_t) * 3 * ((size_t)(kAwTX + 2 * r) + (size_t)(kAwTX + kAwDC - 1 + 2 * r));
+               sizeof(uint32_t) * 3 * ((size_t)(kAwTX + 2 * r) + (size_t)(kAwTX + kAwDC - 1 + 2 * r)) +
+               2 * kAwTX * 4 + 24;
     };
+    CUtensorMap tm{};
     if (half && p.disp_range % 8 != 0) {
         RTS_TRY(go(k_aw_wta<__half, false>, (const __half *)vol));
     } else if (half) {
         const size_t psmem = pipe_smem((size_t)kAwHPitch * 2);
         auto kern = e == 33 ? k_aw_wta_pipe<__half, false, 33> : k_aw_wta_pipe<__half, false, 0>;
         RTS_TRY(set_smem(c, kern, psmem, "aw_wta_pipe"));
-        kern<<<grid, kAwThreads, psmem, c->stream>>>((const __half *)vol, plr, plt, pw, g, raw, rl, cost_out, H, W,
-                                                     p.disp_range, e, 0.f);
+        kern<<<grid, kAwThreads, psmem, c->stream>>>(tm, 0, (const __half *)vol, plr, plt, pw, g, raw, rl, cost_out,
+                                                     H, W, p.disp_range, e, 0.f);
     } else {
-        const size_t psmem = pipe_smem((size_t)kAwCPitch * 4);
+        // dense 64-float cost rows; the tiles whose columns need no wrap take them by TMA
+        const size_t psmem = pipe_smem((size_t)kAwDC * 4);
+        const int use_tma = volume_tensor_map(&tm, vol, H, W, p.disp_range, 4, kAwDC, kAwTX + 2 * r, 1) ? 1 : 0;
         auto kern = e == 33 ? k_aw_wta_pipe<float, true, 33> : k_aw_wta_pipe<float, true, 0>;
         RTS_TRY(set_smem(c, kern, psmem, "aw_wta_pipe"));
-        kern<<<grid, kAwThreads, psmem, c->stream>>>((const float *)vol, plr, plt, pw, g, raw, rl, cost_out, H, W,
-                                                     p.disp_range, e, 0.f);
+        kern<<<grid, kAwThreads, psmem, c->stream>>>(tm, use_tma, (const float *)vol, plr, plt, pw, g, raw, rl,
+                                                     cost_out, H, W, p.disp_range, e, 0.f);
     }
     count_launch(c);
     return check_launch(c, "aw_wta");
