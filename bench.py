@@ -846,7 +846,7 @@ NCU_BYTES_PER_ENTRY = {("cross_vert_wta", 0): 4.16, ("cross_hseg", 0): 4.00,
                        ("cross_vert_wta", 2): 2.13, ("cross_hseg", 2): 2.00}
 # ncu DRAM bytes of one plain-form adaptive-weight launch (k_aw_wta_pipe, one view)
 # at 640x480, D=64 (the full capture of that launch)
-NCU_AW_BYTES = {(640, 480, 64): 85.28e6}
+NCU_AW_BYTES = {(640, 480, 64): 85.31e6}
 # DRAM bytes (read + write) of one k_box_best_dp launch, ncu at 1920x1080, D=128, r=4
 NCU_BOX_BYTES = {(1920, 1080, 128, 4): 1.1375e9}
 
