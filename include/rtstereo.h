@@ -55,6 +55,15 @@ const char *rts_ctx_last_error(const rts_ctx *ctx);
 const char *rts_status_string(rts_status s);
 /* Number of kernels this library has launched since the context was created. */
 uint64_t rts_ctx_kernel_launches(const rts_ctx *ctx);
+/* Fixes the tile of the cross-based view kernels instead of the autotuner's
+ * choice: rows per vertical-aggregation item (a strip of one column), persistent
+ * row-segment blocks per SM, and persistent (1) or one block per item (0);
+ * vert_rows 0 restores the autotuner.  For tests and tuning: every tile gives the
+ * same results. */
+rts_status rts_ctx_force_cross_tune(rts_ctx *ctx, int vert_rows, int grid_mult, int persistent);
+/* Tile copies (TMA) on the context's device whose bounded completion wait gave up
+ * since the library was loaded; their blocks wrote no result.  0 in normal use. */
+uint64_t rts_ctx_tma_timeouts(const rts_ctx *ctx);
 /* Per-stage timing with CUDA events on the context stream (tracing). */
 rts_status rts_ctx_enable_stage_timing(rts_ctx *ctx, int enable);
 /* Copies up to max stage records (name, launches, total ms) accumulated since the

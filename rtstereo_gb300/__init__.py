@@ -136,6 +136,14 @@ class Context:
     def kernel_launches(self) -> int:
         return int(self._lib.rts_ctx_kernel_launches(self.h))
 
+    def force_cross_tune(self, vert_rows: int = 0, grid_mult: int = 8, persistent: int = 0):
+        """Fix the cross-based view kernels' tile (vert_rows 0: the autotuner's choice)."""
+        self.check(self._lib.rts_ctx_force_cross_tune(self.h, vert_rows, grid_mult, persistent), "force_cross_tune")
+
+    def tma_timeouts(self) -> int:
+        """TMA tile copies on this device whose bounded wait gave up (0 in normal use)."""
+        return int(self._lib.rts_ctx_tma_timeouts(self.h))
+
     @property
     def bytes_in_use(self) -> int:
         return int(self._lib.rts_ctx_bytes_in_use(self.h))

@@ -66,6 +66,8 @@ SIGNATURES = {
     "rts_ctx_last_error": (C.c_char_p, [p]),
     "rts_status_string": (C.c_char_p, [i]),
     "rts_ctx_kernel_launches": (u64, [p]),
+    "rts_ctx_tma_timeouts": (u64, [p]),
+    "rts_ctx_force_cross_tune": (i, [p, i, i, i]),
     "rts_ctx_enable_stage_timing": (i, [p, i]),
     "rts_ctx_stage_times": (i, [p, C.POINTER(C.c_char_p), C.POINTER(u64), C.POINTER(d), i]),
     "rts_ctx_reset_stage_times": (None, [p]),

@@ -247,6 +247,10 @@ __device__ __forceinline__ void box_dp_tile(const float2 *bt2, unsigned long lon
 // not landed after kTmaSpin polls counts in g_box_tma_timeouts and its block
 // writes nothing.  Border tiles (wrapped cells) take the cp.async staging.
 __device__ int g_box_tma_timeouts;
+uint64_t box_tma_timeouts() {
+    int v = 0;
+    return cudaMemcpyFromSymbol(&v, g_box_tma_timeouts, sizeof(int)) == cudaSuccess ? (uint64_t)v : 0;
+}
 
 // one tile per block
 template <int R, int POS>

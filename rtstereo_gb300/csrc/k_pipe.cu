@@ -408,6 +408,10 @@ __global__ void __launch_bounds__(kAwThreads, 3) k_aw_wta(const CT *__restrict__
 // E: the window edge as a constant (33, the reference driver's 33 x 33 window), so
 // that the tap loop unrolls whole, or 0 for the edge of the e argument.
 __device__ int g_aw_tma_timeouts;
+uint64_t aw_tma_timeouts() {
+    int v = 0;
+    return cudaMemcpyFromSymbol(&v, g_aw_tma_timeouts, sizeof(int)) == cudaSuccess ? (uint64_t)v : 0;
+}
 
 template <typename CT, bool EXACT, int E>
 __global__ void __launch_bounds__(kAwThreads, 2) k_aw_wta_pipe(const __grid_constant__ CUtensorMap tmap, int use_tma,

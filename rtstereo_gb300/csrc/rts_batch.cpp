@@ -202,7 +202,9 @@ rts_status rts::batch_views_run(rts_ctx *c, int n, const rts_pair *pairs, const 
     // segment storage: exact u16 for integer costs, else by the form; half = 2-byte layout
     const int segk = cross_seg_kind(p, *std::max_element(W.begin(), W.end())), half = segk != 0;
     GraphCache *gc = cache_of(c);
-    const std::string key = shape_key(n, pairs, params);
+    std::string key = shape_key(n, pairs, params);
+    const bool forced = c->force_tune[0] > 0;
+    if (forced) key.append((const char *)c->force_tune, sizeof(c->force_tune));
     const size_t bytes = views_bytes(W.data(), H.data(), D.data(), nv, half);
     void *arena;
     RTS_TRY(scratch(c, SL_BATCH0, bytes, &arena));
@@ -231,6 +233,13 @@ rts_status rts::batch_views_run(rts_ctx *c, int n, const rts_pair *pairs, const 
     fill_views(b, n, pairs, outs, right, p.median_ksize ? &med : nullptr);
     // autotune once per shape: time every candidate on this batch
     auto tit = gc->tunes.find(key);
+    if (tit == gc->tunes.end() && forced) {
+        CrossTune ft;
+        ft.vert_rows = c->force_tune[0];
+        ft.grid_mult = c->force_tune[1];
+        ft.persistent = c->force_tune[2];
+        tit = gc->tunes.emplace(key, ft).first;
+    }
     if (tit == gc->tunes.end()) {
         const bool timing = c->timing;
         c->timing = false;

@@ -190,9 +190,12 @@ rts_status combine_luts(rts_ctx *c, float lambda1, float lambda2, const float **
 }
 
 rts_status combine_lut2d(rts_ctx *c, float lambda1, float lambda2, int trunc, const float **t) {
+    if (trunc < 0 || trunc >= kCombineLut) return set_error(c, RTS_ERR_INVALID_ARG, "combined table: truncation");
     const size_t n = (size_t)(trunc + 1) * 65;
     void *d;
-    RTS_TRY(scratch(c, SL_LUT2D, n * sizeof(float), &d));
+    // the largest table at once: captured CUDA graphs of the cross-based views hold
+    // this address, so the slot must never be reallocated by a larger truncation
+    RTS_TRY(scratch(c, SL_LUT2D, (size_t)kCombineLut * 65 * sizeof(float), &d));
     if (c->lut2d_key.a != lambda1 || c->lut2d_key.b != lambda2 || c->lut2d_key.n != trunc) {
         std::vector<float> tab(n);
         for (int s = 0; s <= trunc; s++) {
@@ -350,6 +353,20 @@ size_t rts_ctx_bytes_in_use(const rts_ctx *c) { return c ? c->used : 0; }
 const char *rts_ctx_last_error(const rts_ctx *c) { return c ? c->last_error.c_str() : "null context"; }
 
 uint64_t rts_ctx_kernel_launches(const rts_ctx *c) { return c ? c->launches.load() : 0; }
+
+rts_status rts_ctx_force_cross_tune(rts_ctx *c, int vert_rows, int grid_mult, int persistent) {
+    if (!c || vert_rows < 0 || (vert_rows > 0 && (grid_mult < 1 || (persistent != 0 && persistent != 1))))
+        return RTS_ERR_INVALID_ARG;
+    c->force_tune[0] = vert_rows;
+    c->force_tune[1] = grid_mult;
+    c->force_tune[2] = persistent;
+    return RTS_OK;
+}
+
+uint64_t rts_ctx_tma_timeouts(const rts_ctx *c) {
+    if (!c || cudaSetDevice(c->device) != cudaSuccess) return 0;
+    return box_tma_timeouts() + aw_tma_timeouts();
+}
 
 rts_status rts_ctx_enable_stage_timing(rts_ctx *c, int enable) {
     if (!c) return RTS_ERR_INVALID_ARG;

@@ -78,6 +78,7 @@ struct rts_ctx {
     bool timing = false;
     std::vector<rts::StageTimer> stages;
     void *graph_cache = nullptr;  // rts::GraphCache*
+    int force_tune[3] = {0, 0, 0};  // cross-based views: {vert_rows, grid_mult, persistent}; vert_rows 0: autotune
 };
 
 namespace rts {
@@ -177,6 +178,9 @@ void launch_cost_log_census(cudaStream_t s, const float *lr, const float *lt, co
                             float lambda1, float lambda2);
 void launch_combine(cudaStream_t s, float *c1, const float *c2, long n, const float *lut1, const float *lut2,
                     float lambda1, float lambda2);
+// TMA copies whose bounded wait gave up (device counters of k_aggr.cu / k_pipe.cu)
+uint64_t box_tma_timeouts();
+uint64_t aw_tma_timeouts();
 // k_aggr.cu
 void launch_box(cudaStream_t s, const float *in, float *out, int H, int W, int D, int r);
 // box mean + WTA winners in one pass (radius 1..8): best[] must hold all ones;

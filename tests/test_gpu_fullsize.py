@@ -164,3 +164,28 @@ def test_fp16_form_agreement(ctx, which):
         agree = (x == y).mean()
         print(f"{which} {name}: {100 * agree:.4f} % equal")
         assert agree >= 0.995, (name, agree)
+
+
+# the cross-based views' tile candidates of the autotuner (csrc/rts_batch.cpp):
+# (rows per vertical item, persistent row blocks per SM, persistent)
+TUNE_CANDIDATES = [(4096, 8, 0), (256, 8, 0), (96, 8, 0), (4096, 8, 1), (256, 8, 1), (4096, 6, 1)]
+
+
+def test_every_cross_tile_matches(ctx, oracle_mod):
+    """Whichever tile the autotuner picks, the 1920x1080 cross-based pair is the
+    oracle's (plain form, bit-exact) and the FP16 form's result is the same."""
+    import rtstereo_gb300 as R
+    O = oracle_mod
+    L, Rr = pair(C2)
+    kw = dict(cost1=1, cost2=3, aggr=3, disp_range=C2["D"])
+    o = O.pipeline(oracle_params(O, R.params(**kw)), L, Rr, O.gray_to_rgb(L), O.gray_to_rgb(Rr))
+    f16 = []
+    try:
+        for t in TUNE_CANDIDATES:
+            ctx.force_cross_tune(*t)
+            assert_pair_equal(ctx.pipeline(R.params(**kw), L, Rr), o, f"plain, tile {t}")
+            f16.append(ctx.pipeline(R.params(precision=R.PREC_F16, **kw), L, Rr))
+    finally:
+        ctx.force_cross_tune(0)
+    for t, g in zip(TUNE_CANDIDATES[1:], f16[1:]):
+        assert_pair_equal(g, f16[0], f"FP16, tile {t} against {TUNE_CANDIDATES[0]}")

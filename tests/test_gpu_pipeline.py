@@ -320,3 +320,31 @@ def test_fp16_form_agrees_with_plain(ctx, kw):
     b = ctx.pipeline(R.params(precision=R.PREC_F16, **kw), L, Rr, Lc, Rc, *lab)
     agree = (a[0] == b[0]).mean()
     assert agree > 0.97, agree
+
+
+def test_tma_tiles_complete(ctx, oracle_mod):
+    """The box and adaptive-weight kernels take their wrap-free tiles by TMA copies
+    with a bounded wait: on shapes with many such tiles the results equal the
+    oracle's and no wait gave up."""
+    L, Rr = synth(0x7A, 160, 48, 64, 4)
+    g, o = run_both(ctx, oracle_mod, L, Rr, disp_range=64, cost1=1, cost2=3, aggr=1, box_rad=4)
+    assert_same(g, o)
+    g, o = run_both(ctx, oracle_mod, L, Rr, want_cost=True, disp_range=64, cost1=1, cost2=3, aggr=2, aw_rad=7)
+    assert_same(g, o)
+    assert ctx.tma_timeouts() == 0
+
+
+def test_cached_graph_after_other_table_sizes(ctx, oracle_mod):
+    """A cross-based pair replays its captured CUDA graph after a configuration
+    with a larger combined cost table (rank + census: 256 rows against AD's 25)
+    ran in between: the replay must still read a live table."""
+    import rtstereo_gb300 as R
+    O = oracle_mod
+    L, Rr = synth(0x61, 160, 40, 64, 4)
+    kw = dict(disp_range=64, aggr=3, cost1=1, cost2=3)
+    first = ctx.pipeline(R.params(**kw), L, Rr)
+    ctx.pipeline(R.params(disp_range=64, aggr=3, cost1=2, cost2=3, rank_rad=3), L, Rr)
+    again = ctx.pipeline(R.params(**kw), L, Rr)
+    o = O.pipeline(O.params(D=64), L, Rr, O.gray_to_rgb(L), O.gray_to_rgb(Rr))
+    assert_same(first, o)
+    assert_same(again, o)
