@@ -15,17 +15,15 @@ namespace rts {
 // dimension) or the driver has no encoder; callers then stage by cp.async.
 inline bool volume_tensor_map(CUtensorMap *m, const void *vol, int H, int W, int D, int elem, int bd, int bw,
                               int bh) {
-    static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
-    static bool tried = false;
-    if (!tried) {
-        tried = true;
+    // looked up once (a function-local static: thread-safe initialisation)
+    static const PFN_cuTensorMapEncodeTiled_v12000 encode = [] {
         void *fn = nullptr;
         cudaDriverEntryPointQueryResult q;
-        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) ==
-                cudaSuccess &&
-            q == cudaDriverEntryPointSuccess)
-            encode = (PFN_cuTensorMapEncodeTiled_v12000)fn;
-    }
+        const bool ok = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault,
+                                                         &q) == cudaSuccess &&
+                        q == cudaDriverEntryPointSuccess;
+        return ok ? (PFN_cuTensorMapEncodeTiled_v12000)fn : (PFN_cuTensorMapEncodeTiled_v12000) nullptr;
+    }();
     if (!encode || ((size_t)D * elem) % 16 != 0 || ((uintptr_t)vol & 15) != 0) return false;
     if (bd > 256 || bw > 256 || bh > 256 || ((size_t)bd * elem) % 16 != 0) return false;
     const cuuint64_t dims[3] = {(cuuint64_t)D, (cuuint64_t)W, (cuuint64_t)H};
