@@ -847,6 +847,9 @@ NCU_BYTES_PER_ENTRY = {("cross_vert_wta", 0): 4.16, ("cross_hseg", 0): 4.00,
 # ncu DRAM bytes of one plain-form adaptive-weight launch (k_aw_wta_pipe, one view)
 # at 640x480, D=64 (the full capture of that launch)
 NCU_AW_BYTES = {(640, 480, 64): 85.31e6}
+# the unit that binds k_aw_wta_pipe (plain form) by the same ncu capture: the SM's
+# L1/shared-memory data pipe (l1tex__data_pipe_lsu_wavefronts, share of its peak)
+NCU_AW_L1_BUSY = {(640, 480, 64): 0.849}
 # DRAM bytes (read + write) of one k_box_best_dp launch, ncu at 1920x1080, D=128, r=4
 NCU_BOX_BYTES = {(1920, 1080, 128, 4): 1.1375e9}
 
@@ -874,12 +877,16 @@ def roofline(stages, name, W, H, D, ag, peaks, src, p, ms_pair=None, sms=152):
         peak = sms * 128 * mhz * 1e6 / 1e12  # one FP32 operation per lane per clock
         traffic = NCU_AW_BYTES.get((W, H, D)) if not p.precision else None
         kern = "k_aw_wta_pipe" if (not p.precision or D % 8 == 0) else "k_aw_wta"
-        return {"bound": "fp32", "kernel": kern, "achieved": achieved, "peak": peak, "unit": "T FP32-pipe op/s",
-                "frac": achieved / peak, "traffic": traffic, "launches": launches, "ms_per_launch": per_launch_ms,
-                "ops_per_launch": ops, "ops_per_tap": ops_per_tap,
-                "peak_source": f"FP32 pipe: {sms} SMs (device attribute) x 128 lanes x {mhz:.0f} MHz "
-                               f"({src} max clock), one operation per lane per clock; no tensor-core or HBM "
-                               f"bound applies (DRAM < 1% busy)"}
+        out = {"bound": "fp32", "kernel": kern, "achieved": achieved, "peak": peak, "unit": "T FP32-pipe op/s",
+               "frac": achieved / peak, "traffic": traffic, "launches": launches, "ms_per_launch": per_launch_ms,
+               "ops_per_launch": ops, "ops_per_tap": ops_per_tap,
+               "peak_source": f"FP32 pipe: {sms} SMs (device attribute) x 128 lanes x {mhz:.0f} MHz "
+                              f"({src} max clock), one operation per lane per clock; no tensor-core or HBM "
+                              f"bound applies (DRAM < 1% busy)"}
+        if not p.precision and (W, H, D) in NCU_AW_L1_BUSY:
+            out["binding_unit"] = {"unit": "L1/shared-memory data pipe", "busy_ncu": NCU_AW_L1_BUSY[(W, H, D)],
+                                   "note": "16-byte shared loads of weights and costs, colour-distance table reads"}
+        return out
     if kname == "box_wta":
         # one launch = one view: (2r+1)^2 sequential FP32 adds per entry (the
         # reference's single chain), no other bound near (the volume read once)

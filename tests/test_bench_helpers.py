@@ -39,6 +39,7 @@ def test_roofline_fields():
     assert r["ops_per_launch"] == pytest.approx(4 * 33 * 33 * 640 * 480 * 64)
     assert r["peak"] == pytest.approx(152 * 128 * 2000e6 / 1e12)
     assert r["frac"] == pytest.approx(r["achieved"] / r["peak"])
+    assert r["binding_unit"]["unit"].startswith("L1") and 0 < r["binding_unit"]["busy_ncu"] <= 1
     # the SM count is the device's (passed in), the FP16 form counts 3 operations a tap
     r16 = bench.roofline({"aw_wta": (2, 8.0)}, "aw_640x480_d64", 640, 480, 64, 2, peaks, "measured",
                          R.params(aggr=2, disp_range=64, precision=R.PREC_F16), sms=160)
