@@ -229,7 +229,7 @@ typedef struct rts_out {
     uint8_t *disp_right; /* [H][W] (right_view) or NULL */
     uint8_t *mask;       /* [H][W] cross-check 0/1 (right_view) or NULL */
     float *cost_left;    /* optional [H][W][D] final left cost volume or NULL (the plain form, or the
-                            FP16 form with adaptive weights of radius <= 16) */
+                            FP16 form with adaptive weights of radius <= 16 or with box aggregation) */
 } rts_out;
 
 rts_status rts_pipeline_run(rts_ctx *, rts_mem, const rts_pair *pair, const rts_params *params, rts_out *out);

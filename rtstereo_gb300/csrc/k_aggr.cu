@@ -172,8 +172,9 @@ __device__ __forceinline__ void box_dp_stage(float2 *bt2, const float *__restric
 
 // the sums, means and per-pixel minimum of one staged tile (warp = tile row)
 template <int R, int POS>
-__device__ __forceinline__ void box_dp_tile(const float2 *bt2, unsigned long long *__restrict__ best, int H, int W,
-                                            int D, int argmax, float rcp_area, int x0, int y0, int d) {
+__device__ __forceinline__ void box_dp_tile(const float2 *bt2, unsigned long long *__restrict__ best,
+                                            float *__restrict__ fin, int H, int W, int D, int argmax, float rcp_area,
+                                            int x0, int y0, int d) {
     constexpr int TW = kBoxDpTX + 2 * R, AREA = (2 * R + 1) * (2 * R + 1);
     constexpr int G = kBoxDpTX;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -214,6 +215,8 @@ __device__ __forceinline__ void box_dp_tile(const float2 *bt2, unsigned long lon
             const float2 q = __ffma2_rn(__ffma2_rn(na, q0, s[m]), ry, q0);
             k0 = (__float_as_uint(q.x) | 0x80000000u) ^ flip;  // wta_key of a float >= +0
             k1 = (__float_as_uint(q.y) | 0x80000000u) ^ flip;
+            // the means themselves where a caller wants the final volume (D even: 8-byte pairs)
+            if (fin && d < D && x < W) *reinterpret_cast<float2 *>(fin + ((size_t)y * W + x) * D + d) = q;
         } else {
             float q[2];
 #pragma unroll
@@ -228,6 +231,8 @@ __device__ __forceinline__ void box_dp_tile(const float2 *bt2, unsigned long lon
             }
             k0 = wta_key(q[0], d, argmax);
             k1 = wta_key(q[1], d + 1, argmax);
+            if (fin && d < D && x < W)
+                *reinterpret_cast<float2 *>(fin + ((size_t)y * W + x) * D + d) = make_float2(q[0], q[1]);
         }
         if (d >= D) k0 = k1 = 0xffffffffu;  // D even: d < D implies d + 1 < D
         // the lane's winner, the lower disparity on a tie
@@ -256,8 +261,9 @@ uint64_t box_tma_timeouts() {
 template <int R, int POS>
 __global__ void __launch_bounds__(256, 2) k_box_best_dp(const __grid_constant__ CUtensorMap tmap, int use_tma,
                                                         const float *__restrict__ vol,
-                                                        unsigned long long *__restrict__ best, int H, int W, int D,
-                                                        int argmax, float rcp_area) {
+                                                        unsigned long long *__restrict__ best,
+                                                        float *__restrict__ fin, int H, int W, int D, int argmax,
+                                                        float rcp_area) {
     constexpr int TW = kBoxDpTX + 2 * R, TH = kBoxDpTY + 2 * R;
     constexpr uint32_t kBytes = (uint32_t)TW * TH * 64 * sizeof(float);
     // [TH][TW][32] pairs; a TMA destination must be 128-byte aligned (checked below:
@@ -284,7 +290,7 @@ __global__ void __launch_bounds__(256, 2) k_box_best_dp(const __grid_constant__ 
         asm volatile("cp.async.wait_all;\n" ::: "memory");
         __syncthreads();
     }
-    box_dp_tile<R, POS>(bt2, best, H, W, D, argmax, rcp_area, x0, y0, d);
+    box_dp_tile<R, POS>(bt2, best, fin, H, W, D, argmax, rcp_area, x0, y0, d);
 }
 
 // per-pixel minimum -> WTA winner word and row summary (see k_wta.cu)
@@ -530,8 +536,9 @@ void launch_box(cudaStream_t s, const float *in, float *out, int H, int W, int D
 }
 bool box_best_supported(int r) { return r >= 1 && r <= 8; }
 
+bool box_best_final_supported(int r, int D) { return box_best_supported(r) && D % 2 == 0 && D > 32; }
 void launch_box_best(cudaStream_t s, const float *vol, unsigned long long *best, uint16_t *raw, int *row_last, int H,
-                     int W, int D, int r, int argmax, int pos) {
+                     int W, int D, int r, int argmax, int pos, float *fin) {
     // disparity pairs for even D above one warp's 32; else a lane per disparity
     const bool dp = D % 2 == 0 && D > 32;
     const dim3 g = dp ? dim3((W + kBoxDpTX - 1) / kBoxDpTX, (H + kBoxDpTY - 1) / kBoxDpTY, (D + 63) / 64)
@@ -548,7 +555,7 @@ void launch_box_best(cudaStream_t s, const float *vol, unsigned long long *best,
         cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         CUtensorMap tm{};
         const int use_tma = volume_tensor_map(&tm, vol, H, W, D, 4, 64, kBoxDpTX + 2 * R, kBoxDpTY + 2 * R) ? 1 : 0;
-        kern<<<g, 256, smem, s>>>(tm, use_tma, vol, best, H, W, D, argmax, rcp_area);
+        kern<<<g, 256, smem, s>>>(tm, use_tma, vol, best, fin, H, W, D, argmax, rcp_area);
     };
 #define RTS_BOX(RR)                                                \
     case RR:                                                       \

@@ -163,7 +163,7 @@ static rts_status cost_volume_composed(rts_ctx *c, const rts_params &p, int H, i
 
 // Composed path for one view: module kernels in the reference's order.
 static rts_status view_composed(rts_ctx *c, const rts_params &p, int H, int W, const ViewIn &v, uint8_t *disp,
-                                int mirror, float *cost_out) {
+                                int mirror, float *cost_out, float *box_means = nullptr) {
     const int D = p.disp_range;
     const size_t np = (size_t)H * W, ne = np * D;
     cudaStream_t s = c->stream;
@@ -208,7 +208,7 @@ static rts_status view_composed(rts_ctx *c, const rts_params &p, int H, int W, c
             // every cost but NCC is >= 0 (absolute differences, distances, 1 - exp(-c/l))
             const bool pos = p.cost1 != RTS_COST_NCC;
             launch_box_best(s, c1, (unsigned long long *)bestv, (uint16_t *)raw, (int *)rl, H, W, D, p.box_rad, argmax,
-                            pos ? 1 : 0);
+                            pos ? 1 : 0, box_means);
             count_launch(c, 2);
         }
         {
@@ -322,10 +322,10 @@ static rts_status view_fused(rts_ctx *c, const rts_params &p, int H, int W, cons
 }
 
 rts_status run_view(rts_ctx *c, const rts_params &p, int H, int W, const ViewIn &v, uint8_t *disp, int mirror,
-                    float *cost_out) {
+                    float *cost_out, float *box_means = nullptr) {
     // the fused kernel also writes the final volume when one is asked for
     if (p.aggr == RTS_AGGR_AW && fused_supported(p, H, W)) return view_fused(c, p, H, W, v, disp, mirror, cost_out);
-    return view_composed(c, p, H, W, v, disp, mirror, cost_out);
+    return view_composed(c, p, H, W, v, disp, mirror, cost_out, box_means);
 }
 
 // Cross-based pipeline of one pair over a view table: both views run in the
@@ -426,11 +426,15 @@ rts_status pipeline_device(rts_ctx *c, const rts_params &p, int H, int W, const 
     }
     if (!cost_out && p.aggr == RTS_AGGR_CROSS && cross_fused_supported(p))
         return pipeline_cross_views(c, p, H, W, lg, rg, lc, rc, dl, dr, mask);
-    // FP16 form, adaptive weights: the right view's final costs are the left view's
-    // read along diagonals (launch_wta_diag), so one aggregation serves both views.
-    // Not for NCC (an arg-max whose products are not symmetric in the two images).
-    const bool shared_right = p.right_view && p.precision == RTS_PREC_F16 && p.aggr == RTS_AGGR_AW &&
-                              p.cost1 != RTS_COST_NCC && p.cost2 != RTS_COST_NCC && fused_supported(p, H, W);
+    // FP16 form, adaptive weights or box: the right view's final costs are the left
+    // view's read along diagonals (launch_wta_diag), so one aggregation serves both
+    // views.  Not for NCC (an arg-max whose products are not symmetric in the two
+    // images).  The box means come from the box + arg-min kernel (even D above 32)
+    // or, when the caller asked for the volume, from the composed path's box.
+    const bool sym = p.cost1 != RTS_COST_NCC && p.cost2 != RTS_COST_NCC;
+    const bool shared_aw = p.aggr == RTS_AGGR_AW && fused_supported(p, H, W);
+    const bool shared_box = p.aggr == RTS_AGGR_BOX && (cost_out || box_best_final_supported(p.box_rad, p.disp_range));
+    const bool shared_right = p.right_view && p.precision == RTS_PREC_F16 && sym && (shared_aw || shared_box);
     float *final_vol = cost_out;
     if (shared_right && !final_vol) {
         void *fv;
@@ -440,7 +444,10 @@ rts_status pipeline_device(rts_ctx *c, const rts_params &p, int H, int W, const 
     {
         StageScope sc(c, "left_view");
         ViewIn v{lg, rg, lc, rc, ll, rl};
-        RTS_TRY(run_view(c, p, H, W, v, dl, 0, final_vol));
+        if (shared_right && p.aggr == RTS_AGGR_BOX && !cost_out)
+            RTS_TRY(run_view(c, p, H, W, v, dl, 0, nullptr, final_vol));
+        else
+            RTS_TRY(run_view(c, p, H, W, v, dl, 0, final_vol));
     }
     if (!p.right_view) return RTS_OK;
     if (shared_right) {
@@ -541,8 +548,11 @@ rts_status rts_pipeline_run(rts_ctx *ctx, rts_mem m, const rts_pair *pair, const
     if (!pair->left_gray || !pair->right_gray || !out->disp_left) return set_error(c, RTS_ERR_INVALID_ARG, "null image or output");
     if (p.right_view && (!out->disp_right || !out->mask)) return set_error(c, RTS_ERR_INVALID_ARG, "right view needs disp_right and mask");
     if (p.aggr == RTS_AGGR_AW && (!pair->left_lab || !pair->right_lab)) return set_error(c, RTS_ERR_INVALID_ARG, "adaptive weights need Lab images");
-    if (out->cost_left && p.precision != RTS_PREC_F32 && !(p.aggr == RTS_AGGR_AW && fused_supported(p, H, W)))
-        return set_error(c, RTS_ERR_INVALID_ARG, "cost_left: the plain form, or the FP16 form of adaptive weights");
+    // (the box path keeps f32 volumes in both forms)
+    if (out->cost_left && p.precision != RTS_PREC_F32 && !(p.aggr == RTS_AGGR_AW && fused_supported(p, H, W)) &&
+        p.aggr != RTS_AGGR_BOX)
+        return set_error(c, RTS_ERR_INVALID_ARG,
+                         "cost_left: the plain form, or the FP16 form of adaptive weights or box aggregation");
     const size_t np = (size_t)H * W, ne = np * p.disp_range;
     const uint8_t *lg, *rg, *lc = nullptr, *rc = nullptr, *ll = nullptr, *rl = nullptr;
     const void *t;

@@ -146,14 +146,14 @@ def test_config3_batch_of_64_mixed_pairs(ctx, oracle_mod):
         assert_pair_equal(g, want, f"pair {i} ({L.shape[1]}x{L.shape[0]}, D={D})")
 
 
-@pytest.mark.parametrize("which", ["c1_aw_640x480", "c2_cross_1920x1080", "c2_aw_1920x1080"])
+@pytest.mark.parametrize("which", ["c1_aw_640x480", "c2_cross_1920x1080", "c2_aw_1920x1080", "c2_box_1920x1080"])
 def test_fp16_form_agreement(ctx, which):
     """FP16 storage with fp32 accumulation: at least 99.5 % of the disparities
     of both views and of the mask equal the plain form's (which is bit-exact to
     the oracle) on the benchmark pairs."""
     import rtstereo_gb300 as R
     cfg, kw = {"c1_aw_640x480": (C1, dict(aggr=2)), "c2_cross_1920x1080": (C2, dict(aggr=3)),
-               "c2_aw_1920x1080": (C2, dict(aggr=2))}[which]
+               "c2_aw_1920x1080": (C2, dict(aggr=2)), "c2_box_1920x1080": (C2, dict(aggr=1, box_rad=4))}[which]
     L, Rr = pair(cfg)
     Lc, Rc = R.gray_to_rgb(L), R.gray_to_rgb(Rr)
     Ll, Rl = R.rgb_to_lab(Lc), R.rgb_to_lab(Rc)

@@ -348,3 +348,28 @@ def test_cached_graph_after_other_table_sizes(ctx, oracle_mod):
     o = O.pipeline(O.params(D=64), L, Rr, O.gray_to_rgb(L), O.gray_to_rgb(Rr))
     assert_same(first, o)
     assert_same(again, o)
+
+
+@pytest.mark.parametrize("W,H,D,rad", [(160, 40, 64, 4), (96, 30, 48, 2), (70, 20, 30, 3)])
+def test_fp16_box_right_view_from_left_volume(ctx, oracle_mod, W, H, D, rad):
+    """FP16 form, box: one aggregation, the right view from the left view's box means
+    along the diagonals (written by the box + arg-min kernel, or by the composed path
+    when the volume is asked for); D = 30 (no disparity-pair kernel) keeps the
+    mirrored right view, equal to the plain form's."""
+    import rtstereo_gb300 as R
+    O = oracle_mod
+    L, Rr = synth(W + 7 * H + D, W, H, D, 4)
+    Lc, Rc = R.gray_to_rgb(L), R.gray_to_rgb(Rr)
+    kw = dict(disp_range=D, aggr=1, box_rad=rad, cost1=1, cost2=3)
+    plain = ctx.pipeline(R.params(**kw), L, Rr, Lc, Rc, want_cost=True)
+    f16 = ctx.pipeline(R.params(precision=R.PREC_F16, **kw), L, Rr, Lc, Rc)
+    f16c = ctx.pipeline(R.params(precision=R.PREC_F16, **kw), L, Rr, Lc, Rc, want_cost=True)
+    assert bits_equal(f16[0], plain[0]) and bits_equal(f16c[0], plain[0]), "left disparity"
+    assert bits_equal(f16c[3], plain[3]), "box means"
+    if D % 2 == 0 and D > 32:
+        want_r = diag_right_view(O, plain[3])
+    else:
+        want_r = plain[1]
+    assert bits_equal(f16[1], want_r), "right disparity (box + arg-min kernel)"
+    assert bits_equal(f16c[1], diag_right_view(O, plain[3])), "right disparity (composed path)"
+    assert bits_equal(f16[2], O.cross_check(f16[0], f16[1])), "cross-check mask"
