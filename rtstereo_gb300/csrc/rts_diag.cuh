@@ -1,18 +1,19 @@
 // rts_diag.cuh -- the right view's local arg-min read from the left view's final
-// volume (the FP16 form of the adaptive-weight pipeline).
+// volume (the FP16 form of the adaptive-weight and box pipelines).
 //
-// In exact arithmetic the adaptive-weight right view's final cost of (pixel x,
-// disparity d) -- the mirrored left-to-right pipeline's -- equals the left
-// view's at ((x + d) mod W, d).  Both are sums over the same taps of the same
-// terms: the product of the same two pixels' weights (zero where either
+// In exact arithmetic the right view's final cost of (pixel x, disparity d) --
+// the mirrored left-to-right pipeline's -- equals the left view's at
+// ((x + d) mod W, d).  Adaptive weights: both are sums over the same taps of the
+// same terms, the product of the same two pixels' weights (zero where either
 // window leaves the image, seq/AdaptiveWeightAggregation.cpp:47-55) times the
 // same symmetric matching cost (AD and census distances do not depend on which
-// image is the reference), the right view's in mirrored tap order.  The FP16
-// form uses this identity; its sums may then round differently from the
-// mirrored pipeline's, so the plain form does not.  (The cross-based sums do
-// not share it: seq/CrossBasedAggregation.cpp:152-153 drops the first cost of a
-// row segment that starts at column 0 of the view, a different column in the
-// mirrored view.)
+// image is the reference).  Box: both windows wrap at the image edges
+// (seq/ConstBlockAggregation.cpp:19-24), so they hold the same costs.  The right
+// view adds them in mirrored tap order.  The FP16 form uses this identity; its
+// sums may then round differently from the mirrored pipeline's, so the plain
+// form does not.  (The cross-based sums do not share it:
+// seq/CrossBasedAggregation.cpp:152-153 drops the first cost of a row segment
+// that starts at column 0 of the view, a different column in the mirrored view.)
 #pragma once
 
 #include "rts_common.cuh"
