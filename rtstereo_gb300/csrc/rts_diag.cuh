@@ -40,9 +40,11 @@ __device__ __forceinline__ void wta_diag_item(const float *__restrict__ vol, uin
     float best = 0.f;
     int win = 0;
     bool found = false;
-    for (int c = 0; 32 * c < D; c++) {
+    // the staged cells of chunk c, loaded into registers one chunk ahead so that
+    // the next chunk's reads are in flight while this one is scanned
+    float v[NI];
+    auto load = [&](int c) {
         const int d = 32 * c + lane;
-        float v[NI];
         // column of staged row i = warp + 8k: one modulo per chunk, then steps of 8
         // wrapped by a subtraction (W >= 8), or by the modulo for narrower images
         int col = (x0 + 32 * c + warp) % W;
@@ -54,6 +56,9 @@ __device__ __forceinline__ void wta_diag_item(const float *__restrict__ vol, uin
             col += kDiagT / 32;
             col = col >= W ? (W >= kDiagT / 32 ? col - W : col % W) : col;
         }
+    };
+    load(0);
+    for (int c = 0; 32 * c < D; c++) {
         __syncthreads();  // the previous chunk's readers are done
 #pragma unroll
         for (int k = 0; k < NI; k++) {
@@ -61,6 +66,7 @@ __device__ __forceinline__ void wta_diag_item(const float *__restrict__ vol, uin
             if (i < kDiagRows) st[i * 33 + lane] = v[k];
         }
         __syncthreads();
+        if (32 * (c + 1) < D) load(c + 1);
         if (x < W) {
             const int jn = imin(32, D - 32 * c);
             for (int j = 0; j < jn; j++) {
