@@ -170,21 +170,29 @@ __device__ __forceinline__ void box_dp_stage(float2 *bt2, const float *__restric
     }
 }
 
-// the sums, means and per-pixel minimum of one staged tile (warp = tile row)
-template <int R, int POS>
-__device__ __forceinline__ void box_dp_tile(const float2 *bt2, unsigned long long *__restrict__ best,
-                                            float *__restrict__ fin, int H, int W, int D, int argmax, float rcp_area,
-                                            int x0, int y0, int d) {
+// The sums, means and per-pixel minimum of one staged tile (warp = tile row).
+// RV (the FP16 form's shared right view): also the right view's minima, for
+// best_r.  The left view's entry (x, d) is the right view's (x - d mod W, d), so
+// after the sums every warp stores its row's keys [16 pixels][64 disparities] in
+// the staging buffer (a barrier first: the other rows' sums read it) and takes,
+// for each of the 79 right pixels x0 - 64 z + k, k in [-63, 15], the minimum of
+// its entries (m, m - k) in increasing disparity, entering {key, d} into best_r.
+template <int R, int POS, bool RV>
+__device__ __forceinline__ void box_dp_tile(float2 *bt2, unsigned long long *__restrict__ best,
+                                            unsigned long long *__restrict__ best_r, int H, int W, int D, int argmax,
+                                            float rcp_area, int x0, int y0, int d) {
     constexpr int TW = kBoxDpTX + 2 * R, AREA = (2 * R + 1) * (2 * R + 1);
     constexpr int G = kBoxDpTX;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int y = y0 + warp;
-    if (y >= H) return;
+    const bool row_ok = y < H;
+    if (!RV && !row_ok) return;
     float2 s[G];
 #pragma unroll
     for (int m = 0; m < G; m++) s[m] = make_float2(0.f, 0.f);
 #pragma unroll
     for (int dy = 0; dy <= 2 * R; dy++) {
+        if (RV && !row_ok) break;
         const float2 *rp = bt2 + (warp + dy) * TW * 32 + lane;
         float2 v[TW];
 #pragma unroll
@@ -193,6 +201,11 @@ __device__ __forceinline__ void box_dp_tile(const float2 *bt2, unsigned long lon
         for (int m = 0; m < G; m++)
 #pragma unroll
             for (int dx = 0; dx <= 2 * R; dx++) s[m] = __fadd2_rn(s[m], v[m + dx]);
+    }
+    uint32_t *const kt = reinterpret_cast<uint32_t *>(bt2) + warp * (G * 64);  // RV: this row's keys
+    if (RV) {
+        __syncthreads();  // every row's sums are done with the staged cells
+        if (!row_ok) return;
     }
     // The mean is sum / AREA correctly rounded (seq/ConstBlockAggregation.cpp:31):
     // q0 = sum * y with y = RN(1 / AREA), the residual r = sum - AREA * q0 by FMA,
@@ -215,8 +228,6 @@ __device__ __forceinline__ void box_dp_tile(const float2 *bt2, unsigned long lon
             const float2 q = __ffma2_rn(__ffma2_rn(na, q0, s[m]), ry, q0);
             k0 = (__float_as_uint(q.x) | 0x80000000u) ^ flip;  // wta_key of a float >= +0
             k1 = (__float_as_uint(q.y) | 0x80000000u) ^ flip;
-            // the means themselves where a caller wants the final volume (D even: 8-byte pairs)
-            if (fin && d < D && x < W) *reinterpret_cast<float2 *>(fin + ((size_t)y * W + x) * D + d) = q;
         } else {
             float q[2];
 #pragma unroll
@@ -231,8 +242,6 @@ __device__ __forceinline__ void box_dp_tile(const float2 *bt2, unsigned long lon
             }
             k0 = wta_key(q[0], d, argmax);
             k1 = wta_key(q[1], d + 1, argmax);
-            if (fin && d < D && x < W)
-                *reinterpret_cast<float2 *>(fin + ((size_t)y * W + x) * D + d) = make_float2(q[0], q[1]);
         }
         if (d >= D) k0 = k1 = 0xffffffffu;  // D even: d < D implies d + 1 < D
         // the lane's winner, the lower disparity on a tie
@@ -241,6 +250,35 @@ __device__ __forceinline__ void box_dp_tile(const float2 *bt2, unsigned long lon
         const uint32_t mn = __reduce_min_sync(0xffffffffu, key);
         const uint32_t bd = __reduce_min_sync(0xffffffffu, key == mn ? kd : 0xffffffffu);
         if (lane == 0 && x < W) atomicMin(best + (size_t)y * W + x, ((unsigned long long)mn << 32) | bd);
+        if (RV) {
+            const bool ok = x < W;  // (k0, k1 are all ones past D)
+            *reinterpret_cast<uint2 *>(kt + m * 64 + 2 * lane) = make_uint2(ok ? k0 : 0xffffffffu, ok ? k1 : 0xffffffffu);
+        }
+    }
+    if (RV) {
+        __syncwarp();
+        const int z64 = d - 2 * lane;  // the block's first disparity
+        for (int rl = lane; rl < G + 63; rl += 32) {
+            const int k = rl - 63;
+            uint32_t bk = 0xffffffffu;
+            int bdl = 0;
+#pragma unroll
+            for (int m = 0; m < G; m++) {
+                const int dl = m - k;
+                if (dl >= 0 && dl < 64) {
+                    const uint32_t kv = kt[m * 64 + dl];
+                    if (kv < bk) {  // strict: the lowest disparity keeps ties
+                        bk = kv;
+                        bdl = dl;
+                    }
+                }
+            }
+            if (bk != 0xffffffffu) {
+                int pr = x0 - z64 + k;  // = x - d of the entries, in (-W, W)
+                if (pr < 0) pr += W;
+                atomicMin(best_r + (size_t)y * W + pr, ((unsigned long long)bk << 32) | (unsigned)(z64 + bdl));
+            }
+        }
     }
 }
 
@@ -258,12 +296,12 @@ uint64_t box_tma_timeouts() {
 }
 
 // one tile per block
-template <int R, int POS>
+template <int R, int POS, bool RV>
 __global__ void __launch_bounds__(256, 2) k_box_best_dp(const __grid_constant__ CUtensorMap tmap, int use_tma,
                                                         const float *__restrict__ vol,
                                                         unsigned long long *__restrict__ best,
-                                                        float *__restrict__ fin, int H, int W, int D, int argmax,
-                                                        float rcp_area) {
+                                                        unsigned long long *__restrict__ best_r, int H, int W, int D,
+                                                        int argmax, float rcp_area) {
     constexpr int TW = kBoxDpTX + 2 * R, TH = kBoxDpTY + 2 * R;
     constexpr uint32_t kBytes = (uint32_t)TW * TH * 64 * sizeof(float);
     // [TH][TW][32] pairs; a TMA destination must be 128-byte aligned (checked below:
@@ -280,7 +318,8 @@ __global__ void __launch_bounds__(256, 2) k_box_best_dp(const __grid_constant__ 
         if (threadIdx.x == 0)
             tma_load_3d((uint32_t)__cvta_generic_to_shared(bt2), &tmap, (int)blockIdx.z * 64, x0 - R, y0 - R, ba,
                         kBytes);
-        if (!mbar_wait(ba, 0)) {
+        // the block decides together, so that no thread waits at a later barrier
+        if (__syncthreads_or(!mbar_wait(ba, 0))) {
             if (threadIdx.x == 0) atomicAdd(&g_box_tma_timeouts, 1);
             mbar_wait(ba, 0);  // the copy may still land in this block's shared memory
             return;
@@ -290,19 +329,21 @@ __global__ void __launch_bounds__(256, 2) k_box_best_dp(const __grid_constant__ 
         asm volatile("cp.async.wait_all;\n" ::: "memory");
         __syncthreads();
     }
-    box_dp_tile<R, POS>(bt2, best, fin, H, W, D, argmax, rcp_area, x0, y0, d);
+    box_dp_tile<R, POS, RV>(bt2, best, best_r, H, W, D, argmax, rcp_area, x0, y0, d);
 }
 
 // per-pixel minimum -> WTA winner word and row summary (see k_wta.cu)
+// (mirror: raw and row_last in the mirrored columns of a right view)
 __global__ void k_best_raw(const unsigned long long *__restrict__ best, uint16_t *__restrict__ raw,
-                           int *__restrict__ row_last, int H, int W) {
+                           int *__restrict__ row_last, int H, int W, int mirror) {
     const int y = blockIdx.y;
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     if (x >= W) return;
     const int win = (int)(best[(size_t)y * W + x] & 0xffffffffu);
     const bool found = win != 0;  // some d >= 1 strictly better than d = 0
-    raw[(size_t)y * W + x] = found ? (uint16_t)(0x100 | win) : (uint16_t)0;
-    if (found) atomicMax(row_last + y, x);
+    const int xo = mirror ? W - 1 - x : x;
+    raw[(size_t)y * W + xo] = found ? (uint16_t)(0x100 | win) : (uint16_t)0;
+    if (found) atomicMax(row_last + y, xo);
 }
 
 // One cross arm (seq/CrossBasedAggregation.cpp:12-100): step outward while the
@@ -536,9 +577,9 @@ void launch_box(cudaStream_t s, const float *in, float *out, int H, int W, int D
 }
 bool box_best_supported(int r) { return r >= 1 && r <= 8; }
 
-bool box_best_final_supported(int r, int D) { return box_best_supported(r) && D % 2 == 0 && D > 32; }
+bool box_best_right_supported(int r, int D) { return box_best_supported(r) && D % 2 == 0 && D > 32; }
 void launch_box_best(cudaStream_t s, const float *vol, unsigned long long *best, uint16_t *raw, int *row_last, int H,
-                     int W, int D, int r, int argmax, int pos, float *fin) {
+                     int W, int D, int r, int argmax, int pos, unsigned long long *best_r) {
     // disparity pairs for even D above one warp's 32; else a lane per disparity
     const bool dp = D % 2 == 0 && D > 32;
     const dim3 g = dp ? dim3((W + kBoxDpTX - 1) / kBoxDpTX, (H + kBoxDpTY - 1) / kBoxDpTY, (D + 63) / 64)
@@ -555,13 +596,16 @@ void launch_box_best(cudaStream_t s, const float *vol, unsigned long long *best,
         cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         CUtensorMap tm{};
         const int use_tma = volume_tensor_map(&tm, vol, H, W, D, 4, 64, kBoxDpTX + 2 * R, kBoxDpTY + 2 * R) ? 1 : 0;
-        kern<<<g, 256, smem, s>>>(tm, use_tma, vol, best, fin, H, W, D, argmax, rcp_area);
+        kern<<<g, 256, smem, s>>>(tm, use_tma, vol, best, best_r, H, W, D, argmax, rcp_area);
     };
 #define RTS_BOX(RR)                                                \
     case RR:                                                       \
-        if (dp) {                                                  \
-            if (pos) go_dp(k_box_best_dp<RR, 1>, RR);              \
-            else go_dp(k_box_best_dp<RR, 0>, RR);                  \
+        if (dp && best_r) {                                        \
+            if (pos) go_dp(k_box_best_dp<RR, 1, true>, RR);        \
+            else go_dp(k_box_best_dp<RR, 0, true>, RR);            \
+        } else if (dp) {                                           \
+            if (pos) go_dp(k_box_best_dp<RR, 1, false>, RR);       \
+            else go_dp(k_box_best_dp<RR, 0, false>, RR);           \
         } else {                                                   \
             if (pos) go(k_box_best<RR, 1>, RR);                    \
             else go(k_box_best<RR, 0>, RR);                        \
@@ -578,7 +622,11 @@ void launch_box_best(cudaStream_t s, const float *vol, unsigned long long *best,
         RTS_BOX(8)
     }
 #undef RTS_BOX
-    k_best_raw<<<row_grid(W, H, 256), 256, 0, s>>>(best, raw, row_last, H, W);
+    k_best_raw<<<row_grid(W, H, 256), 256, 0, s>>>(best, raw, row_last, H, W, 0);
+}
+void launch_best_raw(cudaStream_t s, const unsigned long long *best, uint16_t *raw, int *row_last, int H, int W,
+                     int mirror) {
+    k_best_raw<<<row_grid(W, H, 256), 256, 0, s>>>(best, raw, row_last, H, W, mirror);
 }
 void launch_find_cross(cudaStream_t s, const uint8_t *rgb, int *horz, int *vert, int H, int W, int L, int tau) {
     k_find_cross<<<row_grid(W, H, 128), 128, 0, s>>>(rgb, horz, vert, H, W, L, tau);

@@ -1,5 +1,6 @@
 // rts_diag.cuh -- the right view's local arg-min read from the left view's final
-// volume (the FP16 form of the adaptive-weight and box pipelines).
+// volume (the FP16 form: adaptive weights, and a box whose volume is returned;
+// otherwise the box + arg-min kernel forms the same minima itself).
 //
 // In exact arithmetic the right view's final cost of (pixel x, disparity d) --
 // the mirrored left-to-right pipeline's -- equals the left view's at

@@ -188,10 +188,14 @@ void launch_box(cudaStream_t s, const float *in, float *out, int H, int W, int D
 // is >= 0 (the fast exact division applies)
 bool box_best_supported(int r);
 void launch_box_best(cudaStream_t s, const float *vol, unsigned long long *best, uint16_t *raw, int *row_last, int H,
-                     int W, int D, int r, int argmax, int pos, float *fin = nullptr);
-// launch_box_best can also write the means (the final volume [H][W][D]) to fin:
-// the disparity-pair kernel only (even D above 32)
-bool box_best_final_supported(int r, int D);
+                     int W, int D, int r, int argmax, int pos, unsigned long long *best_r = nullptr);
+// launch_box_best can also enter the right view's minima {key, d} (the left
+// view's entries (x, d) at right pixel x - d mod W) into best_r (all ones at the
+// start): the disparity-pair kernel only (even D above 32)
+bool box_best_right_supported(int r, int D);
+// best [H][W] minima -> raw / row_last (launch_wta_local's), mirrored columns if asked
+void launch_best_raw(cudaStream_t s, const unsigned long long *best, uint16_t *raw, int *row_last, int H, int W,
+                     int mirror);
 void launch_find_cross(cudaStream_t s, const uint8_t *rgb, int *horz, int *vert, int H, int W, int L, int tau);
 // per-channel median of the k x k window, borders replicated (ch 1 or 3)
 inline bool median_ksize_ok(int k) { return k >= 3 && k <= 15 && (k & 1); }

@@ -163,7 +163,7 @@ static rts_status cost_volume_composed(rts_ctx *c, const rts_params &p, int H, i
 
 // Composed path for one view: module kernels in the reference's order.
 static rts_status view_composed(rts_ctx *c, const rts_params &p, int H, int W, const ViewIn &v, uint8_t *disp,
-                                int mirror, float *cost_out, float *box_means = nullptr) {
+                                int mirror, float *cost_out, unsigned long long *box_best_r = nullptr) {
     const int D = p.disp_range;
     const size_t np = (size_t)H * W, ne = np * D;
     cudaStream_t s = c->stream;
@@ -208,7 +208,7 @@ static rts_status view_composed(rts_ctx *c, const rts_params &p, int H, int W, c
             // every cost but NCC is >= 0 (absolute differences, distances, 1 - exp(-c/l))
             const bool pos = p.cost1 != RTS_COST_NCC;
             launch_box_best(s, c1, (unsigned long long *)bestv, (uint16_t *)raw, (int *)rl, H, W, D, p.box_rad, argmax,
-                            pos ? 1 : 0, box_means);
+                            pos ? 1 : 0, box_best_r);
             count_launch(c, 2);
         }
         {
@@ -322,10 +322,10 @@ static rts_status view_fused(rts_ctx *c, const rts_params &p, int H, int W, cons
 }
 
 rts_status run_view(rts_ctx *c, const rts_params &p, int H, int W, const ViewIn &v, uint8_t *disp, int mirror,
-                    float *cost_out, float *box_means = nullptr) {
+                    float *cost_out, unsigned long long *box_best_r = nullptr) {
     // the fused kernel also writes the final volume when one is asked for
     if (p.aggr == RTS_AGGR_AW && fused_supported(p, H, W)) return view_fused(c, p, H, W, v, disp, mirror, cost_out);
-    return view_composed(c, p, H, W, v, disp, mirror, cost_out, box_means);
+    return view_composed(c, p, H, W, v, disp, mirror, cost_out, box_best_r);
 }
 
 // Cross-based pipeline of one pair over a view table: both views run in the
@@ -427,16 +427,24 @@ rts_status pipeline_device(rts_ctx *c, const rts_params &p, int H, int W, const 
     if (!cost_out && p.aggr == RTS_AGGR_CROSS && cross_fused_supported(p))
         return pipeline_cross_views(c, p, H, W, lg, rg, lc, rc, dl, dr, mask);
     // FP16 form, adaptive weights or box: the right view's final costs are the left
-    // view's read along diagonals (launch_wta_diag), so one aggregation serves both
-    // views.  Not for NCC (an arg-max whose products are not symmetric in the two
-    // images).  The box means come from the box + arg-min kernel (even D above 32)
-    // or, when the caller asked for the volume, from the composed path's box.
+    // view's read along diagonals, so one aggregation serves both views.  Not for NCC
+    // (an arg-max whose products are not symmetric in the two images).  Adaptive
+    // weights and a box whose volume the caller asked for: the final volume, then
+    // launch_wta_diag; otherwise the box + arg-min kernel enters the right view's
+    // minima itself (even D above 32).
     const bool sym = p.cost1 != RTS_COST_NCC && p.cost2 != RTS_COST_NCC;
     const bool shared_aw = p.aggr == RTS_AGGR_AW && fused_supported(p, H, W);
-    const bool shared_box = p.aggr == RTS_AGGR_BOX && (cost_out || box_best_final_supported(p.box_rad, p.disp_range));
+    const bool box_rv = p.aggr == RTS_AGGR_BOX && !cost_out && box_best_right_supported(p.box_rad, p.disp_range);
+    const bool shared_box = p.aggr == RTS_AGGR_BOX && (cost_out || box_rv);
     const bool shared_right = p.right_view && p.precision == RTS_PREC_F16 && sym && (shared_aw || shared_box);
     float *final_vol = cost_out;
-    if (shared_right && !final_vol) {
+    unsigned long long *best_r = nullptr;
+    if (shared_right && box_rv) {
+        void *bv;
+        RTS_TRY(scratch(c, SL_V_FINAL, np * 8, &bv));
+        best_r = (unsigned long long *)bv;
+        RTS_CU(c, cudaMemsetAsync(best_r, 0xff, np * 8, s));
+    } else if (shared_right && !final_vol) {
         void *fv;
         RTS_TRY(scratch(c, SL_V_FINAL, np * p.disp_range * 4, &fv));
         final_vol = (float *)fv;
@@ -444,10 +452,7 @@ rts_status pipeline_device(rts_ctx *c, const rts_params &p, int H, int W, const 
     {
         StageScope sc(c, "left_view");
         ViewIn v{lg, rg, lc, rc, ll, rl};
-        if (shared_right && p.aggr == RTS_AGGR_BOX && !cost_out)
-            RTS_TRY(run_view(c, p, H, W, v, dl, 0, nullptr, final_vol));
-        else
-            RTS_TRY(run_view(c, p, H, W, v, dl, 0, final_vol));
+        RTS_TRY(run_view(c, p, H, W, v, dl, 0, final_vol, best_r));
     }
     if (!p.right_view) return RTS_OK;
     if (shared_right) {
@@ -457,7 +462,8 @@ rts_status pipeline_device(rts_ctx *c, const rts_params &p, int H, int W, const 
             RTS_TRY(scratch(c, SL_V_RAW, np * 2, &raw));
             RTS_TRY(scratch(c, SL_V_ROWLAST, (size_t)H * 4, &rlast));
             RTS_CU(c, cudaMemsetAsync(rlast, 0xff, (size_t)H * 4, s));
-            launch_wta_diag(s, final_vol, (uint16_t *)raw, (int *)rlast, H, W, p.disp_range);
+            if (best_r) launch_best_raw(s, best_r, (uint16_t *)raw, (int *)rlast, H, W, 1);
+            else launch_wta_diag(s, final_vol, (uint16_t *)raw, (int *)rlast, H, W, p.disp_range);
             launch_wta_fill(s, (const uint16_t *)raw, (const int *)rlast, dr, H, W, 1);
             count_launch(c, 2);
         }

@@ -352,10 +352,10 @@ def test_cached_graph_after_other_table_sizes(ctx, oracle_mod):
 
 @pytest.mark.parametrize("W,H,D,rad", [(160, 40, 64, 4), (96, 30, 48, 2), (70, 20, 30, 3)])
 def test_fp16_box_right_view_from_left_volume(ctx, oracle_mod, W, H, D, rad):
-    """FP16 form, box: one aggregation, the right view from the left view's box means
-    along the diagonals (written by the box + arg-min kernel, or by the composed path
-    when the volume is asked for); D = 30 (no disparity-pair kernel) keeps the
-    mirrored right view, equal to the plain form's."""
+    """FP16 form, box: one aggregation, the right view the WTA of the left view's box
+    means along the diagonals (the box + arg-min kernel's own minima over the
+    right pixels x - d, or the composed path's volume when it is asked for); D = 30
+    (no disparity-pair kernel) keeps the mirrored right view, the plain form's."""
     import rtstereo_gb300 as R
     O = oracle_mod
     L, Rr = synth(W + 7 * H + D, W, H, D, 4)
