@@ -137,6 +137,11 @@ __global__ void __launch_bounds__(256) k_box_best(const float *__restrict__ vol,
 // directly (no register moves to pair pixels).  A warp takes one tile row, all 16
 // pixels at once; each sum is the reference's single chain as above.
 constexpr int kBoxDpTX = 16, kBoxDpTY = 8;
+// the largest radius box_best_supported admits (8): staged tile + mbarrier
+static_assert((size_t)(kBoxDpTX + 16) * (kBoxDpTY + 16) * 64 * sizeof(float) + 8 <= kSmemOptin,
+              "box pair tile exceeds the shared-memory opt-in");
+static_assert((size_t)(kBoxTX + 16) * (kBoxTY + 16) * 32 * sizeof(float) <= kSmemOptin,
+              "box tile exceeds the shared-memory opt-in");
 
 // cp.async of one tile's cells into bt2 (every cell in flight at once)
 template <int R>

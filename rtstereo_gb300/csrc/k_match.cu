@@ -206,6 +206,8 @@ __global__ void k_window_mean(const uint8_t *__restrict__ img, float *__restrict
 // target values held once (a {tv, tv} pair for a packed multiply would double
 // the shared-memory traffic, which bounds the loop).
 constexpr int kNccTX = 64, kNccTD = 64, kNccTaps = 49;
+static_assert(sizeof(float2) * kNccTaps * kNccTX + sizeof(float) * kNccTaps * (kNccTX + kNccTD) <= kSmemOptin,
+              "NCC tile exceeds the shared-memory opt-in");
 // Reference rows hold float2 values in 16-byte chunks; chunk c is stored at
 // c ^ ((c >> 3) & 1), so the eight 16-byte reads of a quarter warp (4 pixels
 // apart) fall in distinct banks.  A quarter warp's target reads are eight

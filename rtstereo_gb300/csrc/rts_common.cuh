@@ -24,6 +24,10 @@ __device__ __forceinline__ int tar_col(int x, int d, int W, int dir) {
     return t >= W ? t - W : t;
 }
 
+// Dynamic shared memory one block may opt into on sm_100-class GPUs (227 KB);
+// kernels whose tile sizes are compile-time constants assert against it.
+constexpr size_t kSmemOptin = 227 * 1024;
+
 __device__ __forceinline__ int imin(int a, int b) { return a < b ? a : b; }
 __device__ __forceinline__ int imax(int a, int b) { return a > b ? a : b; }
 
