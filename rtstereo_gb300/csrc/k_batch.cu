@@ -392,21 +392,20 @@ template <> struct VRing<__half> {
         asm volatile("ld.shared.u32 %0, [%1+%2];" : "=r"(e) : "r"(a), "n"(OFF));
         return e;
     }
-    static __device__ __forceinline__ float seg(E e) {
-        float f;
-        asm("{\n\t.reg .b16 lo, hi;\n\tmov.b32 {lo, hi}, %1;\n\tcvt.f32.f16 %0, hi;\n\t}" : "=f"(f) : "r"(e));
-        return f;
-    }
+    // the segment enters the f32 sum through the mixed-precision add (f16 operand
+    // widened exactly, one rounding: the same result as converting, then adding)
     static __device__ __forceinline__ void add_if_bit(Acc &a, uint32_t m, uint32_t bit, E e) {
-        asm("{\n\t.reg .pred p;\n\t.reg .b32 t;\n\tand.b32 t, %2, %3;\n\tsetp.ne.u32 p, t, 0;\n\t"
-            "@p add.rn.f32 %0, %0, %4;\n\t@p add.u32 %1, %1, %5;\n\t}"
+        asm("{\n\t.reg .pred p;\n\t.reg .b32 t;\n\t.reg .b16 lo, hi;\n\tand.b32 t, %2, %3;\n\t"
+            "setp.ne.u32 p, t, 0;\n\tmov.b32 {lo, hi}, %4;\n\t"
+            "@p add.rn.f32.f16 %0, hi, %0;\n\t@p add.u32 %1, %1, %4;\n\t}"
             : "+f"(a.s), "+r"(a.c)
-            : "r"(m), "r"(bit), "f"(seg(e)), "r"(e));
+            : "r"(m), "r"(bit), "r"(e));
     }
     static __device__ __forceinline__ void add_if_lt(Acc &a, uint32_t x, uint32_t y, E e) {
-        asm("{\n\t.reg .pred p;\n\tsetp.lo.u32 p, %2, %3;\n\t@p add.rn.f32 %0, %0, %4;\n\t@p add.u32 %1, %1, %5;\n\t}"
+        asm("{\n\t.reg .pred p;\n\t.reg .b16 lo, hi;\n\tsetp.lo.u32 p, %2, %3;\n\tmov.b32 {lo, hi}, %4;\n\t"
+            "@p add.rn.f32.f16 %0, hi, %0;\n\t@p add.u32 %1, %1, %4;\n\t}"
             : "+f"(a.s), "+r"(a.c)
-            : "r"(x), "r"(y), "f"(seg(e)), "r"(e));
+            : "r"(x), "r"(y), "r"(e));
     }
     static __device__ __forceinline__ float sum(Acc a) { return a.s; }
     static __device__ __forceinline__ uint32_t cnt(Acc a) { return a.c & 0xffffu; }
