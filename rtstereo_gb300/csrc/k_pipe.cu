@@ -438,11 +438,13 @@ __global__ void __launch_bounds__(kAwThreads, 2) k_aw_wta_pipe(const __grid_cons
     constexpr int CP = sizeof(CT) == 4 ? kAwDC : kAwHPitch;
     const int CS = (kAwTX + 2 * r + 4) * CP * (int)sizeof(CT) / 4;  // floats of one cost buffer
     // no static shared memory: the dynamic buffers begin at the block's shared base,
-    // as a TMA destination must be 128-byte aligned (checked below all the same)
-    extern __shared__ __align__(128) float asm_[];
-    // buffer b: costs at asm_ + b CS, reference weights at wR0 + b e 64, target weights at wT0 + b e NTP
-    float *const wR0 = asm_ + 2 * CS, *const wT0 = wR0 + 2 * e * kAwTX;
-    uint32_t *labbase = reinterpret_cast<uint32_t *>(asm_ + 2 * CS + 2 * e * kAwTX + 2 * e * NTP);
+    // which the TMA copies need 128-byte aligned (checked per block; blocks whose
+    // base is not take cp.async).  The declaration promises only 16 bytes, the
+    // alignment the compiler's address arithmetic was tuned under.
+    extern __shared__ __align__(16) float psm_[];
+    // buffer b: costs at psm_ + b CS, reference weights at wR0 + b e 64, target weights at wT0 + b e NTP
+    float *const wR0 = psm_ + 2 * CS, *const wT0 = wR0 + 2 * e * kAwTX;
+    uint32_t *labbase = reinterpret_cast<uint32_t *>(psm_ + 2 * CS + 2 * e * kAwTX + 2 * e * NTP);
     const int LRN = kAwTX + 2 * r, LTN = NT + 2 * r;  // words of a reference / target Lab row
     float *const best_v = reinterpret_cast<float *>(labbase + 3 * (LRN + LTN));  // [kAwTX]
     int *const best_i = reinterpret_cast<int *>(best_v + kAwTX);                  // [kAwTX]
@@ -468,7 +470,7 @@ __global__ void __launch_bounds__(kAwThreads, 2) k_aw_wta_pipe(const __grid_cons
     }
     const bool vec = (D & 3) == 0;
     const bool tma_tile = sizeof(CT) == 4 && use_tma && x0 - r >= 0 && x0 + kAwTX + r <= W &&
-                          ((uint32_t)__cvta_generic_to_shared(asm_) & 127) == 0;
+                          ((uint32_t)__cvta_generic_to_shared(psm_) & 127) == 0;
     const uint32_t cb0 = (uint32_t)__cvta_generic_to_shared(cbar);
     uint32_t cphase = 0;  // bit b: parity of the next completion of cbar[b]
     if (tma_tile && tid == 0) {
@@ -512,7 +514,7 @@ __global__ void __launch_bounds__(kAwThreads, 2) k_aw_wta_pipe(const __grid_cons
         // cost rows of tap row ky into C by cp.async (zero fill past D); wrapped
         // columns as in k_aw_wta (seq/AdaptiveWeightAggregation.cpp:95-97)
         auto stage_cost = [&](int ky, int b) {
-            float *C = asm_ + b * CS;
+            float *C = psm_ + b * CS;
             const size_t crow = (size_t)(y + ky) * W;
             const uint32_t cbase = (uint32_t)__cvta_generic_to_shared(C);
             if (tma_tile) {
@@ -650,7 +652,7 @@ __global__ void __launch_bounds__(kAwThreads, 2) k_aw_wta_pipe(const __grid_cons
             if (next) stage_cost(ky + 1, b ^ 1);
             if (ky + 2 <= ky_hi) stage_lab(ky + 2, (i + 2) % 3);
             const int lnext = (i + 1) % 3;
-            const float *Cs = asm_ + b * CS, *wRs = wR0 + b * e * kAwTX, *wTs = wT0 + b * e * NTP;
+            const float *Cs = psm_ + b * CS, *wRs = wR0 + b * e * kAwTX, *wTs = wT0 + b * e * NTP;
             float *wRn = wR0 + (b ^ 1) * e * kAwTX, *wTn = wT0 + (b ^ 1) * e * NTP;
 
             // target weights of entry (j, i): u = px0 + j - (dd0 + i) + 63, so a thread's
@@ -756,7 +758,7 @@ __global__ void __launch_bounds__(kAwThreads, 2) k_aw_wta_pipe(const __grid_cons
             __syncthreads();
         }
         // score / sum of weights (seq/AdaptiveWeightAggregation.cpp:108), staged for the arg-min
-        float *outs = asm_;  // [64][kAwDC + 1]
+        float *outs = psm_;  // [64][kAwDC + 1]
 #pragma unroll
         for (int j = 0; j < 4; j++)
 #pragma unroll

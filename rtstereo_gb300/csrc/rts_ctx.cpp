@@ -137,7 +137,9 @@ StageScope::StageScope(rts_ctx *c_, const char *name) : c(c_), idx(-1) {
     for (size_t i = 0; i < c->stages.size(); i++)
         if (c->stages[i].name == name) idx = (int)i;
     if (idx < 0) {
-        c->stages.push_back(StageTimer{name});
+        StageTimer st;
+        st.name = name;
+        c->stages.push_back(st);
         idx = (int)c->stages.size() - 1;
     }
     if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
