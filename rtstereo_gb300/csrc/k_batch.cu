@@ -197,7 +197,7 @@ constexpr int kHSub = 8;    // columns per group
 // table (the configuration of the cross-based pipeline), 2 any AD/census pair,
 // 3 census alone, 4 truncated AD alone (integer costs, u16 segments)
 template <typename ST, int MODE, int GRAYREC>
-__global__ void __launch_bounds__(kHsegW * 32, 8) k_hseg_views(ViewTable t, CostCfg cfg, const float *__restrict__ lut2d) {
+__global__ void __launch_bounds__(kHsegW * 32, 8) k_hseg_views(ViewTable t, CostCfg cfg) {
     __shared__ __align__(16) float pring[kHsegW][64][32];
     __shared__ uint32_t lring[kHsegW][32][32];
     __shared__ uint4 recA[kHsegW][32];
@@ -263,15 +263,16 @@ __global__ void __launch_bounds__(kHsegW * 32, 8) k_hseg_views(ViewTable t, Cost
                     if constexpr (MODE == 0) {
                         cv[u] = vol[(size_t)imin(hx + u, W - 1) * D];
                     } else if constexpr (MODE == 1) {
-                        // CombineCost of min(SAD, trunc) and the Hamming distance: one host-made
-                        // table of T1[s] + T2[h] (seq/CombineCost.cpp:21-23)
+                        // CombineCost of min(SAD, trunc) and the Hamming distance: the float add of
+                        // the two host-made terms T1[s] + T2[h] (seq/CombineCost.cpp:21-23), two
+                        // small tables a warp's lanes read in a few L1 lines
                         // the first cost: colour AD (truncated), or the AD of the ranks
                         // (seq/PixelBasedCost.cpp:13-24 on rank images)
                         int s = GRAYREC == 2 ? abs((int)a.z - (int)b.z)
                                 : GRAYREC ? abs((int)a.z - (int)b.z) * 3 : (int)__vsadu4(a.z, b.z);
                         s = imin(s, cfg.itrunc);
                         const int hd = __popc(a.x ^ b.x) + __popc(a.y ^ b.y);
-                        cv[u] = __ldg(lut2d + s * 65 + hd);
+                        cv[u] = __fadd_rn(__ldg(cfg.lut1 + s), __ldg(cfg.lut2 + hd));
                     } else if constexpr (MODE == 3) {
                         // census alone: the Hamming distance (seq/CensusTransform.cpp:39-62)
                         cv[u] = (float)(__popc(a.x ^ b.x) + __popc(a.y ^ b.y));
@@ -751,7 +752,7 @@ static bool mode1(const rts_params &p) {
                     p.ad_trunc == floorf(p.ad_trunc);
     return (ad || (p.cost1 == RTS_COST_RANK && p.rank_rad <= 16)) && p.cost2 == RTS_COST_CENSUS;
 }
-// the largest first-cost value of the table path
+// the largest first-cost value of the table path (its truncation)
 static int mode1_smax(const rts_params &p) { return p.cost1 == RTS_COST_RANK ? 255 : (int)p.ad_trunc; }
 
 // The largest cost of a configuration whose costs are all integers (census
@@ -784,8 +785,7 @@ bool cross_record_costs(const rts_params &p) {
 
 rts_status cross_tables(rts_ctx *c, const rts_params &p) {
     const float *t;
-    if (mode1(p)) RTS_TRY(combine_lut2d(c, p.lambda1, p.lambda2, mode1_smax(p), &t));
-    else if (p.cost2 != RTS_COST_NONE) {
+    if (p.cost2 != RTS_COST_NONE) {
         const float *t2;
         RTS_TRY(combine_luts(c, p.lambda1, p.lambda2, &t, &t2));
     }
@@ -810,11 +810,9 @@ rts_status launch_cross_views(rts_ctx *c, const rts_params &p, const ViewTable &
     cfg.int_path = trunc_ok ? 1 : 0;
     cfg.itrunc = cfg.trunc1 ? (int)p.ad_trunc : 0x7fffffff;
     const int mode = has_vol ? 0 : mode1(p) ? 1 : 2;
-    const float *lut2d = nullptr, *rcp = nullptr;
-    if (mode == 1) {
-        RTS_TRY(combine_lut2d(c, p.lambda1, p.lambda2, mode1_smax(p), &lut2d));
-        cfg.itrunc = mode1_smax(p);
-    } else if (p.cost2 != RTS_COST_NONE) RTS_TRY(combine_luts(c, p.lambda1, p.lambda2, &cfg.lut1, &cfg.lut2));
+    const float *rcp = nullptr;
+    if (mode == 1) cfg.itrunc = mode1_smax(p);
+    if (p.cost2 != RTS_COST_NONE) RTS_TRY(combine_luts(c, p.lambda1, p.lambda2, &cfg.lut1, &cfg.lut2));
     RTS_TRY(recip_table(c, &rcp));
     const bool rank = mode == 1 && p.cost1 == RTS_COST_RANK;
     // record colour word: 2 rank, 1 gray byte, 0 packed RGB
@@ -848,7 +846,7 @@ rts_status launch_cross_views(rts_ctx *c, const rts_params &p, const ViewTable &
     {
         StageScope sc(c, "cross_hseg");
         const unsigned g = grid(t.total[ST_HSEG], kHsegW, tune.grid_mult);
-        auto go = [&](auto kern) { kern<<<g, kHsegW * 32, 0, s>>>(t, cfg, lut2d); };
+        auto go = [&](auto kern) { kern<<<g, kHsegW * 32, 0, s>>>(t, cfg); };
         if (segk == 2) {
             // integer costs: census alone, or truncated AD alone
             if (p.cost1 == RTS_COST_CENSUS) go(k_hseg_views<uint16_t, 3, 0>);

@@ -191,32 +191,6 @@ rts_status combine_luts(rts_ctx *c, float lambda1, float lambda2, const float **
     return RTS_OK;
 }
 
-rts_status combine_lut2d(rts_ctx *c, float lambda1, float lambda2, int trunc, const float **t) {
-    if (trunc < 0 || trunc >= kCombineLut) return set_error(c, RTS_ERR_INVALID_ARG, "combined table: truncation");
-    const size_t n = (size_t)(trunc + 1) * 65;
-    void *d;
-    // the largest table at once: captured CUDA graphs of the cross-based views hold
-    // this address, so the slot must never be reallocated by a larger truncation
-    RTS_TRY(scratch(c, SL_LUT2D, (size_t)kCombineLut * 65 * sizeof(float), &d));
-    if (c->lut2d_key.a != lambda1 || c->lut2d_key.b != lambda2 || c->lut2d_key.n != trunc) {
-        std::vector<float> tab(n);
-        for (int s = 0; s <= trunc; s++) {
-            const float t1 = 1 - expf(-(float)s / lambda1);  // seq/CombineCost.cpp:21-22
-            for (int h = 0; h <= 64; h++) {
-                const float t2 = 1 - expf(-(float)h / lambda2);
-                tab[(size_t)s * 65 + h] = t1 + t2;  // :23
-            }
-        }
-        RTS_CU(c, cudaMemcpyAsync(d, tab.data(), n * sizeof(float), cudaMemcpyHostToDevice, c->stream));
-        RTS_CU(c, cudaStreamSynchronize(c->stream));
-        c->lut2d_key.a = lambda1;
-        c->lut2d_key.b = lambda2;
-        c->lut2d_key.n = trunc;
-    }
-    *t = (const float *)d;
-    return RTS_OK;
-}
-
 rts_status recip_table(rts_ctx *c, const float **r) {
     void *d;
     RTS_TRY(scratch(c, SL_RCP, (kRecipMax + 1) * sizeof(float), &d));

@@ -25,7 +25,7 @@ enum Slot {
     SL_IN0, SL_IN1, SL_IN2, SL_IN3, SL_IN4, SL_IN5,
     SL_OUT0, SL_OUT1, SL_OUT2,
     SL_TMP0, SL_TMP1, SL_TMP2, SL_TMP3,
-    SL_LUT0, SL_LUT1, SL_LUTW, SL_PW, SL_LUT2D, SL_RCP,
+    SL_LUT0, SL_LUT1, SL_LUTW, SL_PW, SL_RCP,
     // pipeline, per view
     SL_V_GRAY, SL_V_RGB, SL_V_LAB,          // view-ordered copies of the inputs (both images)
     SL_V_CODES, SL_V_ARMS, SL_V_AUX,        // census codes, packed arms, rank/LoG images
@@ -69,7 +69,6 @@ struct rts_ctx {
     std::vector<rts::DevBuf> extra;  // batch / server buffers
     // cached host-computed lookup tables (the key is what the table was made for)
     rts::LutKey lut_key[2];
-    rts::LutKey lut2d_key;
     bool rcp_ready = false;
     float lutw_gamma = -1.f;
     float pw_gamma = -1.f;
@@ -141,9 +140,6 @@ template <typename K> rts_status set_smem(rts_ctx *c, K kern, size_t smem, const
 // host-computed tables (glibc expf/sqrtf, same as the reference) ----------
 // combine LUT: T[v] = 1 - expf(-(float)v / lambda), v in [0, kCombineLut)
 rts_status combine_luts(rts_ctx *c, float lambda1, float lambda2, const float **l1, const float **l2);
-// combined table T[s * 65 + h] = T1[s] + T2[h] of a truncated AD s in [0, trunc]
-// and a Hamming distance h in [0, 64] (the float add of seq/CombineCost.cpp:23)
-rts_status combine_lut2d(rts_ctx *c, float lambda1, float lambda2, int trunc, const float **t);
 // correctly rounded reciprocals R[n] = 1 / (float)n, n in [1, kRecipMax]
 constexpr int kRecipMax = 47 * 47;  // largest cross of arm 23: (2 * 23 + 1)^2 pixels
 rts_status recip_table(rts_ctx *c, const float **r);

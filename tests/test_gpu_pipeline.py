@@ -336,8 +336,8 @@ def test_tma_tiles_complete(ctx, oracle_mod):
 
 def test_cached_graph_after_other_table_sizes(ctx, oracle_mod):
     """A cross-based pair replays its captured CUDA graph after a configuration
-    with a larger combined cost table (rank + census: 256 rows against AD's 25)
-    ran in between: the replay must still read a live table."""
+    with other cost tables (rank + census: first costs up to 255 against AD's
+    24) ran in between: the replay must still read live tables."""
     import rtstereo_gb300 as R
     O = oracle_mod
     L, Rr = synth(0x61, 160, 40, 64, 4)
