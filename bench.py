@@ -16,6 +16,8 @@ W*H*D per pair-step (both views) / time.
                form, disparity agreement, cost error against FP64 on sampled rows
   c2_cross_1080p (default line) the 1920x1080, D=128 cross-based pipeline, plain and
                FP16 forms, against the stage model's HBM roofline
+  c2_box_1080p (default line) the 1920x1080, D=128 box 9x9 pipeline, plain and FP16
+               forms (the FP16 form aggregates once for both views)
   serve        (default line) a Poisson stream of mixed pairs through the serving loop
                at --serve-rate pairs/s: per-size p50/p99 and pairs/s
   --impl reference  the CPU implementation (oracle/_ref if built here, else the oracle
@@ -720,6 +722,21 @@ def c2_cross_record(bench, peaks):
                     "stages_ms_per_step": m16["stages_ms_per_step"], "clocks": m16["clocks"]}}
 
 
+def c2_box_record(bench):
+    """The 1920x1080, D=128 box 9x9 pipeline, plain and FP16 forms: the FP16 form
+    aggregates once and its box + arg-min kernel also forms the right view's
+    minima (x - d), the plain form runs the mirrored pipeline for the right view."""
+    name = "box_1920x1080_d128"
+    m = bench.measure(name, "f32")
+    m16 = bench.measure(name, "f16")
+    return {"workload": name, "ms_per_pair": m["ms"], "value": m["value"], "unit": "MDE/s",
+            "e2e_ms_per_pair": m["e2e"]["ms_per_step"], "stages_ms_per_step": m["stages_ms_per_step"],
+            "dominant_kernel": m["roofline"], "clocks": m["clocks"],
+            "f16": {"ms_per_pair": m16["ms"], "value": m16["value"], "ratio_to_plain": m16["value"] / m["value"],
+                    "agreement": agreement(m["out"], m16["out"]), "stages_ms_per_step": m16["stages_ms_per_step"],
+                    "clocks": m16["clocks"]}}
+
+
 def f16_record(bench, plain):
     """The FP16 form of the same workload as the line's plain run."""
     import rtstereo_gb300 as R
@@ -804,11 +821,12 @@ def run_ours(args, rank, world):
     m = bench.measure(args.workload, args.precision)
     extra = {}
     # the other target figures ride on the default line (one GPU): the FP16 form,
-    # the 1920x1080 cross-based pipeline, and the serving loop
+    # the 1920x1080 cross-based and box pipelines, and the serving loop
     if world == 1 and args.workload == DEFAULT and args.precision == "f32" and not args.no_extra:
         peaks, _ = measured_peaks()
         extra["f16"] = f16_record(bench, m)
         extra["c2_cross_1080p"] = c2_cross_record(bench, peaks)
+        extra["c2_box_1080p"] = c2_box_record(bench)
         srv = serve_measure(bench.ctx, args.serve_rate, args.requests, args.budget_gb, args.max_batch,
                             args.priority_pixels, "f16", world)
         extra["serve"] = {k: srv[k] for k in ("value", "unit", "offered_per_s", "requests", "latency_target",
@@ -960,7 +978,7 @@ def main():
     ap.add_argument("--module-path", action="store_true",
                     help="time the drop-in module path (seq-signature calls, HOST buffers) on the workload")
     ap.add_argument("--no-extra", action="store_true",
-                    help="default workload: skip the f16 / c2_cross_1080p / serve sub-records")
+                    help="default workload: skip the f16 / c2_cross_1080p / c2_box_1080p / serve sub-records")
     ap.add_argument("--serve-rate", type=float, default=600.0,
                     help="offered rate (pairs/s) of the serve sub-record of the default line")
     args = ap.parse_args()
