@@ -36,13 +36,6 @@ __global__ void k_box(const float *__restrict__ in, float *__restrict__ out, int
 // comparisons (a NaN never wins, a NaN at d = 0 blocks every other d, -0 == +0).
 constexpr int kBoxTX = 32, kBoxTY = 8;
 
-__device__ __forceinline__ uint32_t wta_key(float v, int d, int argmax) {
-    if (v != v) return d == 0 ? 0u : 0xffffffffu;
-    uint32_t u = __float_as_uint(__fadd_rn(v, 0.0f));  // -0 -> +0
-    u = (u & 0x80000000u) ? ~u : (u | 0x80000000u);
-    return argmax ? ~u : u;
-}
-
 template <int R, int POS>
 __global__ void __launch_bounds__(256) k_box_best(const float *__restrict__ vol, unsigned long long *__restrict__ best,
                                                   int H, int W, int D, int argmax, float rcp_area) {

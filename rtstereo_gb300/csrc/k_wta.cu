@@ -5,36 +5,59 @@
 // has no strictly better d >= 1 than d = 0 keeps the previous pixel's winner
 // (raster order, across rows).  On the GPU this is two passes:
 //   1. k_wta_local: per pixel, the first strict arg-min (arg-max) and whether
-//      any d >= 1 won ("found"); found pixels raise row_last[y] to their x;
+//      any d >= 1 won ("found"); found pixels raise row_last[y] to their x.
+//      Warp per pixel, lane = disparity, so a warp reads its pixel's D costs
+//      as whole lines; the winner is the least {wta_key, d};
 //   2. k_wta_fill: one warp per row takes the incoming winner from the nearest
 //      earlier row that has a found pixel, then propagates within the row with
 //      a ballot scan.
 // raw[p] = found ? 0x100 | winner : 0.  row_last must start at -1.
+#include <algorithm>
+
 #include "rts_common.cuh"
 #include "rts_diag.cuh"
 
 namespace rts {
 
-__global__ void k_wta_local(const float *__restrict__ cost, uint16_t *__restrict__ raw, int *__restrict__ row_last,
-                            int H, int W, int D, int argmax) {
-    const int y = blockIdx.y;
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    if (x >= W) return;
-    const float *c = cost + ((size_t)y * W + x) * D;
-    float best = c[0];
-    int win = 0;
-    bool found = false;
-    for (int d = 1; d < D; d++) {
-        const float v = c[d];
-        const bool better = argmax ? (v > best) : (v < best);
-        if (better) {
-            best = v;
-            win = d;
-            found = true;
+constexpr int kWtaWarps = 8, kWtaPix = 4;  // warps of a block; pixels of a warp at a time
+__global__ void __launch_bounds__(kWtaWarps * 32) k_wta_local(const float *__restrict__ cost, uint16_t *__restrict__ raw,
+                                                              int *__restrict__ row_last, int H, int W, int D,
+                                                              int argmax) {
+    const int lane = threadIdx.x & 31;
+    const long np = (long)H * W;
+    // resident blocks stride over the pixels, a warp kWtaPix consecutive pixels at a
+    // time, every pixel's loads of a 32-disparity step in flight together
+    const long stride = (long)gridDim.x * kWtaWarps * kWtaPix;
+    for (long p0 = ((long)blockIdx.x * kWtaWarps + (threadIdx.x >> 5)) * kWtaPix; p0 < np; p0 += stride) {
+        uint32_t bk[kWtaPix], bd[kWtaPix];
+#pragma unroll
+        for (int j = 0; j < kWtaPix; j++) bk[j] = bd[j] = 0xffffffffu;
+#pragma unroll 2
+        for (int d = lane; d < D; d += 32) {
+            float v[kWtaPix];
+#pragma unroll
+            for (int j = 0; j < kWtaPix; j++) v[j] = __ldg(cost + (p0 + j < np ? p0 + j : np - 1) * D + d);
+#pragma unroll
+            for (int j = 0; j < kWtaPix; j++) {
+                const uint32_t k = wta_key(v[j], d, argmax);
+                if (k < bk[j]) {  // a lane's d increase: a tie keeps the lower
+                    bk[j] = k;
+                    bd[j] = (uint32_t)d;
+                }
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < kWtaPix; j++) {
+            const uint32_t mn = __reduce_min_sync(0xffffffffu, bk[j]);
+            const uint32_t win = __reduce_min_sync(0xffffffffu, bk[j] == mn ? bd[j] : 0xffffffffu);
+            const long p = p0 + j;
+            if (lane == 0 && p < np) {
+                const bool found = win != 0;  // some d >= 1 strictly better than d = 0
+                raw[p] = found ? (uint16_t)(0x100 | win) : (uint16_t)0;
+                if (found) atomicMax(row_last + p / W, (int)(p % W));
+            }
         }
     }
-    raw[(size_t)y * W + x] = found ? (uint16_t)(0x100 | win) : (uint16_t)0;
-    if (found) atomicMax(row_last + y, x);
 }
 
 __global__ void k_wta_fill(const uint16_t *__restrict__ raw, const int *__restrict__ row_last,
@@ -102,7 +125,16 @@ __global__ void k_flip(const uint8_t *__restrict__ in, uint8_t *__restrict__ out
 
 void launch_wta_local(cudaStream_t s, const float *cost, uint16_t *raw, int *row_last, int H, int W, int D,
                       int argmax) {
-    k_wta_local<<<dim3((W + 127) / 128, H), 128, 0, s>>>(cost, raw, row_last, H, W, D, argmax);
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = 132;
+    }
+    const long np = (long)H * W, per_block = (long)kWtaWarps * kWtaPix;
+    const long blocks = std::min((np + per_block - 1) / per_block, (long)sms * 8);
+    k_wta_local<<<(unsigned)blocks, kWtaWarps * 32, 0, s>>>(cost, raw, row_last, H, W, D, argmax);
 }
 void launch_wta_diag(cudaStream_t s, const float *vol, uint16_t *raw, int *row_last, int H, int W, int D) {
     k_wta_diag<<<dim3((W + kDiagT - 1) / kDiagT, H), kDiagT, 0, s>>>(vol, raw, row_last, W, D);

@@ -29,6 +29,18 @@ __device__ __forceinline__ int tar_col(int x, int d, int W, int dir) {
 constexpr size_t kSmemOptin = 227 * 1024;
 
 __device__ __forceinline__ int imin(int a, int b) { return a < b ? a : b; }
+
+// WTA order key of cost v at disparity d (seq/WTA.cpp:10-39): the least {key, d}
+// over d is the reference's winner -- the first strict minimum (maximum with
+// argmax) in increasing d.  Keys order like the floats, -0 == +0; a NaN never wins
+// (the largest key), and a NaN at d = 0 blocks every other d (the smallest key,
+// which no number takes).
+__device__ __forceinline__ uint32_t wta_key(float v, int d, int argmax) {
+    if (v != v) return d == 0 ? 0u : 0xffffffffu;
+    uint32_t u = __float_as_uint(__fadd_rn(v, 0.0f));  // -0 -> +0
+    u = (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+    return argmax ? ~u : u;
+}
 __device__ __forceinline__ int imax(int a, int b) { return a > b ? a : b; }
 
 // Packed cross arms of one pixel: left | right<<8 | top<<16 | bottom<<24.
