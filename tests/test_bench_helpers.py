@@ -120,3 +120,27 @@ def test_latency_target_record():
     assert bench.latency_target(by, "1280x720", 5.0) is None
     by["1920x1080"]["p99"] = 5.0
     assert bench.latency_target(by, "1920x1080", 5.0)["met"] is False
+
+
+def test_c2_box_record_fields():
+    """The default line's box sub-record from two measured runs (a stand-in for the
+    GPU measurement): the FP16 ratio, the agreement of both views and the mask."""
+    import bench
+    outs = [np.full((4, 6), 7, np.uint8), np.full((4, 6), 5, np.uint8), np.ones((4, 6), np.uint8)]
+
+    class FakeBench:
+        def measure(self, name, precision):
+            assert name == "box_1920x1080_d128"
+            ms = 2.34 if precision == "f32" else 1.30
+            o16 = [a.copy() for a in outs]
+            if precision == "f16":
+                o16[1][0, 0] = 6  # one right-view disparity differs
+            return {"ms": ms, "value": 1920 * 1080 * 128 / 1e6 / (ms / 1e3), "e2e": {"ms_per_step": ms + 0.1},
+                    "stages_ms_per_step": {"box_wta": ms / 2}, "roofline": {"kernel": "k_box_best_dp", "frac": 0.77},
+                    "clocks": {"sm_mhz": 2070.0}, "out": o16}
+
+    r = bench.c2_box_record(FakeBench())
+    assert r["workload"] == "box_1920x1080_d128" and r["ms_per_pair"] == pytest.approx(2.34)
+    assert r["dominant_kernel"]["kernel"] == "k_box_best_dp"
+    assert r["f16"]["ratio_to_plain"] == pytest.approx(2.34 / 1.30)
+    assert r["f16"]["agreement"] == {"disp_left": 1.0, "disp_right": pytest.approx(23 / 24), "mask": 1.0}
